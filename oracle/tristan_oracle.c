@@ -1,0 +1,1111 @@
+/*
+ * CPU oracle for the TRISTAN-MP per-step PIC hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker): the tests, the smoke check and
+ * bench.py's CPU-baseline leg call it; the GPU product path never does.
+ *
+ * Each function restates one reference subroutine in the reference's own
+ * floating-point operation order (left-to-right Fortran evaluation, one
+ * rounding per operation, no FMA). File:line citations are to
+ * mrowan137/tristan-mp-pu-master_densdecomp.
+ *
+ * Parity status: "parity unpinned" against reference outputs (the reference
+ * ships no golden vectors and no Fortran toolchain exists to run it). The
+ * restatement is pinned by an independent pure-Python transliteration
+ * (tests/golden/make_golden.py, bit-exact agreement required) and by
+ * physics known-answer tests (tests/test_oracle_physics.py).
+ *
+ * Choices where the reference is undefined, stated once here:
+ *  - densdecomp_1ord never initialises curx_add_prev / cury_add_prevs
+ *    (code/particles.F90:717-732); they are taken as 0 here, as the 2nd and
+ *    3rd order routines initialise them (:907-910, :1155-1158).
+ *  - pind is never zeroed for ions before first use (code/particles.F90:319,
+ *    particles_movedeposit.F90:1544 commented out); it is taken as 0.
+ *  - the shape-mismatched copy at code/fieldboundaries.F90:1938 folds the
+ *    full nghost/2+1 rows of cury by default; TO_QUIRK_Q5_LHS reproduces the
+ *    left-hand-side-extent reading instead.
+ */
+#include "tristan_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* shape-function constants as code/particles.F90:235-248 computes them in
+   single precision */
+#define HALF 0.5f
+#define ONE 1.0f
+#define TWO 2.0f
+#define QUART 0.25f
+#define NINEIGHTH 1.125f
+#define THHALF 1.5f
+#define NEGONE (-1.0f)
+static const float TWOTH = 2.0f / 3.0f;
+static const float THIRD = 1.0f / 3.0f;
+static const float SIXTH = 1.0f / 6.0f;
+static const float NEGSIXTH = -(1.0f / 6.0f);
+
+int to_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int64_t to_lot(const to_state *s) { return (int64_t)s->mx * s->my * s->mz; }
+
+/* 0-based linear index of the 1-based Fortran cell (i,j,k) */
+static inline int64_t L3(const to_state *s, int64_t i, int64_t j, int64_t k)
+{
+    return (i - 1) + (int64_t)s->mx * ((j - 1) + (int64_t)s->my * (k - 1));
+}
+
+/* ------------------------------------------------------------------------
+ * Shape factors. S is indexed by the reference's slot number 1..6; slot 3
+ * holds the weight of node aint(x). `off` is the slot shift used by the
+ * deposit for the new position (Sx2(3+shifti) ...). Sets [*mn,*mxs].
+ * Orders: code/particles.F90:738-745 (1st), :928-1020 (2nd),
+ * :1175-1277 (3rd); identical forms in the movers
+ * (code/particles_movedeposit.F90:447-468, :709-790, :1035-1128).
+ * --------------------------------------------------------------------- */
+static void shape(int order, float d, float *S, int off, int *mn, int *mxs)
+{
+    if (order == 1) {
+        S[3 + off] = ONE - d;
+        S[4 + off] = d;
+        *mn = 3 + off;
+        *mxs = 4 + off;
+    } else if (order == 2) {
+        if (d <= HALF) {
+            S[2 + off] = HALF * (d * d - d + QUART);
+            S[4 + off] = S[2 + off] + d;
+            S[3 + off] = ONE - S[4 + off] - S[2 + off];
+            *mn = 2 + off;
+            *mxs = 4 + off;
+        } else if (d > HALF) {
+            S[3 + off] = NINEIGHTH - THHALF * d + HALF * d * d;
+            S[5 + off] = S[3 + off] - ONE + d;
+            S[4 + off] = ONE - S[5 + off] - S[3 + off];
+            *mn = 3 + off;
+            *mxs = 5 + off;
+        }
+    } else {
+        if (d <= HALF) {
+            S[2 + off] = NEGSIXTH * (d - ONE) * (d - ONE) * (d - ONE);
+            S[3 + off] = TWOTH + HALF * (d - TWO) * d * d;
+            S[5 + off] = SIXTH * d * d * d;
+            S[4 + off] = ONE - S[5 + off] - S[3 + off] - S[2 + off];
+        } else if (d > HALF) {
+            S[5 + off] = SIXTH * d * d * d;
+            S[4 + off] = TWOTH + HALF * (NEGONE - d) * (ONE - d) * (ONE - d);
+            S[2 + off] = SIXTH * (ONE - d) * (ONE - d) * (ONE - d);
+            S[3 + off] = ONE - S[5 + off] - S[4 + off] - S[2 + off];
+        }
+        *mn = 2 + off;
+        *mxs = 5 + off;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Movers: mover_1ord / mover_2ord / mover_3ord
+ * (code/particles_movedeposit.F90:356-610, :619-933, :943-1271).
+ * The loop ranges are the dual shape's (the dual assignment overwrites the
+ * primal iter*min/max), which truncates the 2nd-order primal weights (Q1).
+ * 2D gathers from the staggered Yee arrays with mixed primal/dual weights;
+ * 3D gathers from primal-averaged copies with primal weights (Q2, Q3).
+ * --------------------------------------------------------------------- */
+typedef struct {
+    float *ex_p, *ey_p, *ez_p, *bx_p, *by_p, *bz_p;
+} primal_fields;
+
+/* primal grids, code/particles_movedeposit.F90:395-404 (cshift wraps over
+   the full local array, ghosts included) */
+static void make_primal(const to_state *s, primal_fields *pf)
+{
+    int64_t lot = to_lot(s);
+    int mx = s->mx, my = s->my, mz = s->mz;
+    pf->ex_p = malloc(sizeof(float) * lot);
+    pf->ey_p = malloc(sizeof(float) * lot);
+    pf->ez_p = malloc(sizeof(float) * lot);
+    pf->bx_p = malloc(sizeof(float) * lot);
+    pf->by_p = malloc(sizeof(float) * lot);
+    pf->bz_p = malloc(sizeof(float) * lot);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= mz; k++) {
+        int km = (k == 1) ? mz : k - 1;
+        for (int j = 1; j <= my; j++) {
+            int jm = (j == 1) ? my : j - 1;
+            for (int i = 1; i <= mx; i++) {
+                int im = (i == 1) ? mx : i - 1;
+                int64_t l = L3(s, i, j, k);
+                pf->ex_p[l] = 0.5f * (s->ex[l] + s->ex[L3(s, im, j, k)]);
+                pf->ey_p[l] = 0.5f * (s->ey[l] + s->ey[L3(s, i, jm, k)]);
+                pf->ez_p[l] = 0.5f * (s->ez[l] + s->ez[L3(s, i, j, km)]);
+                pf->bx_p[l] = 0.5f * (s->bx[l] + s->bx[L3(s, i, jm, k)]);
+                pf->by_p[l] = 0.5f * (s->by[l] + s->by[L3(s, im, j, k)]);
+                pf->bz_p[l] = 0.5f * (0.5f * (s->bz[l] + s->bz[L3(s, im, j, k)]) +
+                                      0.5f * (s->bz[L3(s, i, jm, k)] + s->bz[L3(s, im, jm, k)]));
+            }
+        }
+    }
+}
+
+static void free_primal(primal_fields *pf)
+{
+    free(pf->ex_p); free(pf->ey_p); free(pf->ez_p);
+    free(pf->bx_p); free(pf->by_p); free(pf->bz_p);
+}
+
+static void push_one(const to_state *s, const primal_fields *pf, to_particle *pp, float qm)
+{
+    const float c = s->c;
+    const float cinv = 1.0f / c;
+    const int order = s->order;
+    const int64_t iy = s->mx, iz = (int64_t)s->mx * s->my;
+    float Sxp[8], Syp[8], Szp[8], Sxd[8], Syd[8], Szd[8];
+    int i1min, i1max, i2min, i2max, i3min = 0, i3max = -1;
+    memset(Sxp, 0, sizeof Sxp); memset(Syp, 0, sizeof Syp); memset(Szp, 0, sizeof Szp);
+    memset(Sxd, 0, sizeof Sxd); memset(Syd, 0, sizeof Syd); memset(Szd, 0, sizeof Szd);
+
+    const float x = pp->x, y = pp->y, z = pp->z;
+    int ip = (int)truncf(x);
+    float dxp = x - (float)ip;
+    int jp = (int)truncf(y);
+    float dyp = y - (float)jp;
+    int kp = (int)truncf(z);
+    int id = (int)truncf(x - HALF);
+    float dxd = x - HALF - (float)id;
+    int jd = (int)truncf(y - HALF);
+    float dyd = y - HALF - (float)jd;
+    int kd = (int)truncf(z - HALF);
+    float dzp = 0.0f, dzd = 0.0f;
+    if (s->dims == 3) {
+        dzp = z - (float)kp;
+        dzd = (z - HALF) - (float)kd;
+    }
+    int dmy;
+    /* primal first, then dual: the dual's ranges are the ones kept */
+    shape(order, dxp, Sxp, 0, &i1min, &i1max);
+    shape(order, dyp, Syp, 0, &i2min, &i2max);
+    if (s->dims == 3) shape(order, dzp, Szp, 0, &i3min, &i3max);
+    shape(order, dxd, Sxd, 0, &i1min, &i1max);
+    shape(order, dyd, Syd, 0, &i2min, &i2max);
+    if (s->dims == 3) shape(order, dzd, Szd, 0, &i3min, &i3max);
+    (void)dmy;
+
+    float ex0 = 0.0f, ey0 = 0.0f, ez0 = 0.0f, bx0 = 0.0f, by0 = 0.0f, bz0 = 0.0f;
+    if (s->dims == 3) {
+        for (int it3 = i3min; it3 <= i3max; it3++) {
+            for (int it2 = i2min; it2 <= i2max; it2++) {
+                int64_t jj = jp - 3 + it2, kk = kp - 3 + it3;
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f, sbx = 0.0f, sby = 0.0f, sbz = 0.0f;
+                for (int it1 = i1min; it1 <= i1max; it1++) {
+                    int64_t l = L3(s, ip - 3 + it1, jj, kk);
+                    sx = sx + pf->ex_p[l] * Sxp[it1];
+                    sy = sy + pf->ey_p[l] * Sxp[it1];
+                    sz = sz + pf->ez_p[l] * Sxp[it1];
+                    sbx = sbx + pf->bx_p[l] * Sxp[it1];
+                    sby = sby + pf->by_p[l] * Sxp[it1];
+                    sbz = sbz + pf->bz_p[l] * Sxp[it1];
+                }
+                ex0 = ex0 + sx * Syp[it2] * Szp[it3];
+                ey0 = ey0 + sy * Syp[it2] * Szp[it3];
+                ez0 = ez0 + sz * Syp[it2] * Szp[it3];
+                bx0 = bx0 + sbx * Syp[it2] * Szp[it3];
+                by0 = by0 + sby * Syp[it2] * Szp[it3];
+                bz0 = bz0 + sbz * Syp[it2] * Szp[it3];
+            }
+        }
+    } else {
+        for (int it2 = i2min; it2 <= i2max; it2++) {
+            for (int it1 = i1min; it1 <= i1max; it1++) {
+                /* 1-based linear indices as the reference builds them */
+                int64_t lpp = (ip - 3 + it1) + iy * (jp - 3 + it2 - 1);
+                int64_t lpd = (ip - 3 + it1) + iy * (jd - 3 + it2 - 1);
+                int64_t ldp = (id - 3 + it1) + iy * (jp - 3 + it2 - 1);
+                int64_t ldd = (id - 3 + it1) + iy * (jd - 3 + it2 - 1);
+                ex0 = ex0 + s->ex[ldp - 1] * Sxd[it1] * Syp[it2];
+                ey0 = ey0 + s->ey[lpd - 1] * Sxp[it1] * Syd[it2];
+                ez0 = ez0 + s->ez[lpp - 1] * Sxp[it1] * Syp[it2];
+                bx0 = bx0 + s->bx[lpd - 1] * Sxp[it1] * Syd[it2];
+                by0 = by0 + s->by[ldp - 1] * Sxd[it1] * Syp[it2];
+                bz0 = bz0 + s->bz[ldd - 1] * Sxd[it1] * Syd[it2];
+            }
+        }
+    }
+    (void)iz;
+
+    ex0 = 0.5f * ex0 * qm;
+    ey0 = 0.5f * ey0 * qm;
+    ez0 = 0.5f * ez0 * qm;
+    bx0 = 0.5f * bx0 * qm * cinv;
+    by0 = 0.5f * by0 * qm * cinv;
+    bz0 = 0.5f * bz0 * qm * cinv;
+
+    if (s->external_fields) {
+        bx0 = bx0 + s->ext[3] * 0.5f * qm * cinv;
+        by0 = by0 + s->ext[4] * 0.5f * qm * cinv;
+        bz0 = bz0 + s->ext[5] * 0.5f * qm * cinv;
+        ex0 = ex0 + s->ext[0] * 0.5f * qm;
+        ey0 = ey0 + s->ext[1] * 0.5f * qm;
+        ez0 = ez0 + s->ext[2] * 0.5f * qm;
+    }
+
+    /* Boris, code/particles_movedeposit.F90:564-583 */
+    float u0 = c * pp->u + ex0;
+    float v0 = c * pp->v + ey0;
+    float w0 = c * pp->w + ez0;
+    float g = c / sqrtf(c * c + u0 * u0 + v0 * v0 + w0 * w0);
+    bx0 = g * bx0;
+    by0 = g * by0;
+    bz0 = g * bz0;
+    float f = 2.0f / (1.0f + bx0 * bx0 + by0 * by0 + bz0 * bz0);
+    float u1 = (u0 + v0 * bz0 - w0 * by0) * f;
+    float v1 = (v0 + w0 * bx0 - u0 * bz0) * f;
+    float w1 = (w0 + u0 * by0 - v0 * bx0) * f;
+    u0 = u0 + v1 * bz0 - w1 * by0 + ex0;
+    v0 = v0 + w1 * bx0 - u1 * bz0 + ey0;
+    w0 = w0 + u1 * by0 - v1 * bx0 + ez0;
+    pp->u = u0 * cinv;
+    pp->v = v0 * cinv;
+    pp->w = w0 * cinv;
+    /* position advance, :602-606 */
+    g = c / sqrtf(c * c + u0 * u0 + v0 * v0 + w0 * w0);
+    pp->x = pp->x + pp->u * g * c;
+    pp->y = pp->y + pp->v * g * c;
+    pp->z = pp->z + pp->w * g * c;
+}
+
+void to_mover(to_state *s, int64_t n1, int64_t n2, float qm)
+{
+    primal_fields pf = {0};
+    if (s->dims == 3) make_primal(s, &pf);
+#pragma omp parallel for schedule(static)
+    for (int64_t n = n1; n < n2; n++) push_one(s, &pf, &s->p[n], qm);
+    if (s->dims == 3) free_primal(&pf);
+}
+
+/* code/particles_movedeposit.F90:63-88 */
+void to_move_particles(to_state *s)
+{
+    to_mover(s, 0, s->ions, s->qmi);
+    to_mover(s, s->maxhlf, s->maxhlf + s->lecs, s->qme);
+}
+
+/* ------------------------------------------------------------------------
+ * Esirkepov deposit, densdecomp_{1,2,3}ord (code/particles.F90:678-1358).
+ * The x carry (curx_add_prev) is not reset between rows, and the y carries
+ * (cury_add_prevs) not between planes (Q4). `acc` receives each addition:
+ * FP32 into cur*, or int64 fixed point.
+ * --------------------------------------------------------------------- */
+typedef struct {
+    float *cx, *cy, *cz;
+    int64_t *fx, *fy, *fz;
+    float scale;
+    int64_t lot;
+    int fixed;
+} dep_target;
+
+static inline void dep_add(const dep_target *t, int comp, int64_t l, float v)
+{
+    if (l < 0 || l >= t->lot) return; /* the reference writes out of bounds */
+    if (t->fixed) {
+        int64_t q = llrintf(v * t->scale);
+        if (comp == 0) t->fx[l] += q;
+        else if (comp == 1) t->fy[l] += q;
+        else t->fz[l] += q;
+    } else {
+        if (comp == 0) t->cx[l] = t->cx[l] + v;
+        else if (comp == 1) t->cy[l] = t->cy[l] + v;
+        else t->cz[l] = t->cz[l] + v;
+    }
+}
+
+static void densdecomp(const to_state *s, const dep_target *t, float x2, float y2, float z2,
+                       float x1, float y1, float z1, float q)
+{
+    const int order = s->order;
+    const int64_t iy = s->mx, iz = (int64_t)s->mx * s->my;
+    float Sx1[8], Sy1[8], Sx2[8], Sy2[8], Sz1[8], Sz2[8];
+    float cury_adds[8], cury_add_prevs[8], curz_adds[8][8], curz_add_prevs[8][8];
+    float curx_add = 0.0f, curx_add_prev = 0.0f, curz_add = 0.0f;
+    memset(Sx1, 0, sizeof Sx1); memset(Sx2, 0, sizeof Sx2);
+    memset(Sy1, 0, sizeof Sy1); memset(Sy2, 0, sizeof Sy2);
+    memset(Sz1, 0, sizeof Sz1); memset(Sz2, 0, sizeof Sz2);
+    memset(cury_adds, 0, sizeof cury_adds); memset(cury_add_prevs, 0, sizeof cury_add_prevs);
+    memset(curz_adds, 0, sizeof curz_adds); memset(curz_add_prevs, 0, sizeof curz_add_prevs);
+
+    int i1 = (int)truncf(x1), i2 = (int)truncf(x2);
+    int j1 = (int)truncf(y1), j2 = (int)truncf(y2);
+    int k1 = (int)truncf(z1), k2 = (int)truncf(z2);
+    int shifti = i2 - i1, shiftj = j2 - j1, shiftk = k2 - k1;
+    float dx1 = x1 - truncf(x1), dy1 = y1 - truncf(y1);
+    float dx2 = x2 - truncf(x2), dy2 = y2 - truncf(y2);
+    float dz1 = z1 - truncf(z1), dz2 = z2 - truncf(z2);
+    float deltaz = z2 - z1;
+    if (s->dims == 2) { k1 = 1; k2 = 1; shiftk = 0; }
+    (void)k2;
+
+    int x1mn, x1mx, x2mn, x2mx, y1mn, y1mx, y2mn, y2mx, z1mn = 0, z1mx = 0, z2mn = 0, z2mx = 0;
+    shape(order, dx1, Sx1, 0, &x1mn, &x1mx);
+    shape(order, dy1, Sy1, 0, &y1mn, &y1mx);
+    if (s->dims == 3) shape(order, dz1, Sz1, 0, &z1mn, &z1mx);
+    shape(order, dx2, Sx2, shifti, &x2mn, &x2mx);
+    shape(order, dy2, Sy2, shiftj, &y2mn, &y2mx);
+    if (s->dims == 3) shape(order, dz2, Sz2, shiftk, &z2mn, &z2mx);
+    int xmn = x1mn < x2mn ? x1mn : x2mn, xmx = x1mx > x2mx ? x1mx : x2mx;
+    int ymn = y1mn < y2mn ? y1mn : y2mn, ymx = y1mx > y2mx ? y1mx : y2mx;
+
+    if (s->dims == 3) {
+        int zmn = z1mn < z2mn ? z1mn : z2mn, zmx = z1mx > z2mx ? z1mx : z2mx;
+        for (int it2 = zmn; it2 <= zmx; it2++) {
+            for (int it1 = ymn; it1 <= ymx; it1++) {
+                for (int it = xmn; it <= xmx; it++) {
+                    int64_t l2 = (i1 - 3 + it) + (int64_t)(j1 - 3 + it1 - 1) * iy +
+                                 (int64_t)(k1 - 3 + it2 - 1) * iz;
+                    curx_add = q * ((Sx2[it] - Sx1[it]) *
+                                    (Sy1[it1] * Sz1[it2] + HALF * (Sy2[it1] - Sy1[it1]) * Sz1[it2] +
+                                     HALF * Sy1[it1] * (Sz2[it2] - Sz1[it2]) +
+                                     THIRD * (Sy2[it1] - Sy1[it1]) * (Sz2[it2] - Sz1[it2]))) +
+                               curx_add_prev;
+                    cury_adds[it] = q * ((Sy2[it1] - Sy1[it1]) *
+                                         (Sx1[it] * Sz1[it2] + HALF * (Sx2[it] - Sx1[it]) * Sz1[it2] +
+                                          HALF * Sx1[it] * (Sz2[it2] - Sz1[it2]) +
+                                          THIRD * (Sx2[it] - Sx1[it]) * (Sz2[it2] - Sz1[it2]))) +
+                                    cury_add_prevs[it];
+                    curz_adds[it][it1] = q * ((Sz2[it2] - Sz1[it2]) *
+                                              (Sx1[it] * Sy1[it1] + HALF * (Sx2[it] - Sx1[it]) * Sy1[it1] +
+                                               HALF * Sx1[it] * (Sy2[it1] - Sy1[it1]) +
+                                               THIRD * (Sx2[it] - Sx1[it]) * (Sy2[it1] - Sy1[it1]))) +
+                                         curz_add_prevs[it][it1];
+                    dep_add(t, 0, l2 - 1, curx_add);
+                    dep_add(t, 1, l2 - 1, cury_adds[it]);
+                    dep_add(t, 2, l2 - 1, curz_adds[it][it1]);
+                    curx_add_prev = curx_add;
+                }
+                curx_add = 0.0f;
+                memcpy(cury_add_prevs, cury_adds, sizeof cury_adds);
+                memset(cury_adds, 0, sizeof cury_adds);
+            }
+            memcpy(curz_add_prevs, curz_adds, sizeof curz_adds);
+            memset(curz_adds, 0, sizeof curz_adds);
+        }
+    } else {
+        for (int it1 = ymn; it1 <= ymx; it1++) {
+            for (int it = xmn; it <= xmx; it++) {
+                int64_t l2 = (i1 - 3 + it) + (int64_t)(j1 - 3 + it1 - 1) * iy;
+                curx_add = q * ((Sx2[it] - Sx1[it]) * (Sy1[it1] + HALF * (Sy2[it1] - Sy1[it1]))) +
+                           curx_add_prev;
+                cury_adds[it] = q * ((Sy2[it1] - Sy1[it1]) * (Sx1[it] + HALF * (Sx2[it] - Sx1[it]))) +
+                                cury_add_prevs[it];
+                curz_add = -(q * deltaz *
+                             (Sx1[it] * Sy1[it1] + HALF * (Sx2[it] - Sx1[it]) * Sy1[it1] +
+                              HALF * Sx1[it] * (Sy2[it1] - Sy1[it1]) +
+                              THIRD * (Sx2[it] - Sx1[it]) * (Sy2[it1] - Sy1[it1])));
+                dep_add(t, 0, l2 - 1, curx_add);
+                dep_add(t, 1, l2 - 1, cury_adds[it]);
+                dep_add(t, 2, l2 - 1, curz_add);
+                curx_add_prev = curx_add;
+            }
+            curx_add = 0.0f;
+            memcpy(cury_add_prevs, cury_adds, sizeof cury_adds);
+            memset(cury_adds, 0, sizeof cury_adds);
+        }
+    }
+    (void)curz_add;
+}
+
+static dep_target make_target(to_state *s)
+{
+    dep_target t;
+    t.cx = s->curx; t.cy = s->cury; t.cz = s->curz;
+    t.fx = s->fx; t.fy = s->fy; t.fz = s->fz;
+    t.scale = ldexpf(1.0f, s->fx_shift);
+    t.lot = to_lot(s);
+    t.fixed = s->fixed;
+    return t;
+}
+
+void to_densdecomp(to_state *s, float x2, float y2, float z2, float x1, float y1, float z1, float q)
+{
+    dep_target t = make_target(s);
+    densdecomp(s, &t, x2, y2, z2, x1, y1, z1, q);
+}
+
+void to_fixed_to_float(to_state *s)
+{
+    int64_t lot = to_lot(s);
+    double inv = ldexp(1.0, -s->fx_shift);
+#pragma omp parallel for schedule(static)
+    for (int64_t l = 0; l < lot; l++) {
+        s->curx[l] = (float)((double)s->fx[l] * inv);
+        s->cury[l] = (float)((double)s->fy[l] * inv);
+        s->curz[l] = (float)((double)s->fz[l] * inv);
+    }
+}
+
+/* the per-species deposit loop (:1381-1540 ions, :1715-1880 electrons):
+   reconstruct the old position from the new one and the new momentum */
+static void deposit_species(to_state *s, int64_t base, int64_t count, float qs)
+{
+    const float c = s->c;
+#ifdef _OPENMP
+    int nth = omp_get_max_threads();
+    if (nth > 1 && count > 4096) {
+        /* thread-private accumulators, summed in thread order; the serial
+           build (used for parity) never takes this branch */
+        int64_t lot = to_lot(s);
+        float *pcur = NULL;
+        int64_t *pfix = NULL;
+        if (s->fixed) pfix = calloc((size_t)nth * 3 * lot, sizeof(int64_t));
+        else pcur = calloc((size_t)nth * 3 * lot, sizeof(float));
+#pragma omp parallel
+        {
+            int tid = omp_get_thread_num();
+            dep_target t = make_target(s);
+            if (s->fixed) {
+                t.fx = pfix + (size_t)tid * 3 * lot; t.fy = t.fx + lot; t.fz = t.fy + lot;
+            } else {
+                t.cx = pcur + (size_t)tid * 3 * lot; t.cy = t.cx + lot; t.cz = t.cy + lot;
+            }
+#pragma omp for schedule(static)
+            for (int64_t n = 0; n < count; n++) {
+                to_particle *pp = &s->p[base + n];
+                float invgam = 1.0f / sqrtf(1.0f + pp->u * pp->u + pp->v * pp->v + pp->w * pp->w);
+                float x0 = pp->x - pp->u * invgam * c;
+                float y0 = pp->y - pp->v * invgam * c;
+                float z0 = pp->z - pp->w * invgam * c;
+                float q = pp->ch * qs;
+                densdecomp(s, &t, pp->x, pp->y, pp->z, x0, y0, z0, q);
+            }
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t l = 0; l < lot; l++) {
+            for (int th = 0; th < nth; th++) {
+                size_t b = (size_t)th * 3 * lot;
+                if (s->fixed) {
+                    s->fx[l] += pfix[b + l]; s->fy[l] += pfix[b + lot + l]; s->fz[l] += pfix[b + 2 * lot + l];
+                } else {
+                    s->curx[l] += pcur[b + l]; s->cury[l] += pcur[b + lot + l]; s->curz[l] += pcur[b + 2 * lot + l];
+                }
+            }
+        }
+        free(pcur);
+        free(pfix);
+        return;
+    }
+#endif
+    dep_target t = make_target(s);
+    for (int64_t n = 0; n < count; n++) {
+        to_particle *pp = &s->p[base + n];
+        float invgam = 1.0f / sqrtf(1.0f + pp->u * pp->u + pp->v * pp->v + pp->w * pp->w);
+        float x0 = pp->x - pp->u * invgam * c;
+        float y0 = pp->y - pp->v * invgam * c;
+        float z0 = pp->z - pp->w * invgam * c;
+        float q = pp->ch * qs;
+        densdecomp(s, &t, pp->x, pp->y, pp->z, x0, y0, z0, q);
+    }
+}
+
+/* boundary loop of deposit_particles (:1546-1691 ions, :1884-2026
+   electrons) for one rank (sizex = sizey = 1): periodic wrap by
+   +-(max-min), discard outside [x1in,x2in] on open axes, and in 3D the
+   z-crossing particles routed to the z out-lists (MPI to self) */
+static void boundary_species(to_state *s, int64_t base, int64_t *count, int64_t *nout,
+                             to_particle **dwn, int64_t *ndwn, to_particle **up, int64_t *nup)
+{
+    const int nghost = s->nghost, nghostz = s->nghostz;
+    const float maxx = (float)s->mx - 1.0f * (float)(nghost / 2);
+    const float minx = 1.0f * (float)(nghost / 2 + 1);
+    const float maxy = (float)s->my - 1.0f * (float)(nghost / 2);
+    const float miny = 1.0f * (float)(nghost / 2 + 1);
+    float maxz, minz;
+    if (s->dims == 3) {
+        maxz = (float)s->mz - 1.0f * (float)(nghostz / 2);
+        minz = 1.0f * (float)(nghostz / 2 + 1);
+    } else {
+        minz = 1.0f * (float)(nghostz / 2 + 1);
+        maxz = 1.0f * (float)(nghostz / 2 + 1) + 1.0f;
+    }
+    const float midx = 0.5f * (maxx - minx), midy = 0.5f * (maxy - miny), midz = 0.5f * (maxz - minz);
+    int64_t n0 = *count;
+    *ndwn = 0;
+    *nup = 0;
+    *dwn = NULL;
+    *up = NULL;
+    if (n0 > 0 && s->dims == 3) {
+        *dwn = malloc(sizeof(to_particle) * n0);
+        *up = malloc(sizeof(to_particle) * n0);
+    }
+    for (int64_t n = 0; n < n0; n++) {
+        to_particle *pp = &s->p[base + n];
+        int in = 1;
+        float perx = 0.0f, pery = 0.0f, perz = 0.0f;
+        if (pp->x < minx || pp->x > maxx) perx = copysignf(midx, pp->x - minx) + copysignf(midx, pp->x - maxx);
+        if (pp->y < miny || pp->y > maxy) pery = copysignf(midy, pp->y - miny) + copysignf(midy, pp->y - maxy);
+        if (pp->z < minz || pp->z > maxz) perz = copysignf(midz, pp->z - minz) + copysignf(midz, pp->z - maxz);
+        if (s->periodic[0] == 0) {
+            float xg = pp->x + (float)s->mxcum;
+            in = ((double)xg > s->x1in) && ((double)xg < s->x2in);
+        }
+        if (s->periodic[1] == 0 && in) {
+            float yg = pp->y + (float)s->mycum;
+            in = ((double)yg > s->y1in) && ((double)yg < s->y2in);
+        }
+        if (s->dims == 3 && s->periodic[2] == 0 && in) {
+            float zg = pp->z + (float)s->mzcum;
+            in = ((double)zg > s->z1in) && ((double)zg < s->z2in);
+        }
+        if (!in) { perx = 0.0f; pery = 0.0f; perz = 0.0f; }
+        pp->x = pp->x - perx;
+        pp->y = pp->y - pery;
+        if (s->dims == 3) {
+            if (perz != 0.0f && in) { in = 0; perx = 0.0f; pery = 0.0f; }
+            if (perz < 0.0f) perz = -((float)s->mz - 1.0f * (float)nghostz);
+        }
+        pp->z = pp->z - perz;
+        if (in) continue;
+        (*nout)++;
+        if (s->dims == 3) {
+            if (perz < 0.0f) (*dwn)[(*ndwn)++] = *pp;
+            if (perz > 0.0f) (*up)[(*nup)++] = *pp;
+        }
+        s->pind[n] = 1;
+    }
+    /* compaction: swap from the end (:1694-1705, :2029-2040) */
+    int64_t cnt = n0;
+    for (int64_t n = 0; n < n0; n++) {
+        while (s->pind[n] != 0) {
+            s->p[base + n] = s->p[base + cnt - 1];
+            s->pind[n] = s->pind[cnt - 1];
+            s->pind[cnt - 1] = 0;
+            cnt--;
+        }
+    }
+    *count = cnt;
+}
+
+void to_deposit_particles(to_state *s)
+{
+    s->nionout = 0;
+    s->nlecout = 0;
+    if (s->ions > 0) deposit_species(s, 0, s->ions, s->qi);
+    if (s->lecs > 0) deposit_species(s, s->maxhlf, s->lecs, s->qe);
+    to_particle *idwn = NULL, *iup = NULL, *ldwn = NULL, *lup = NULL;
+    int64_t nidwn = 0, niup = 0, nldwn = 0, nlup = 0;
+    if (s->ions > 0) boundary_species(s, 0, &s->ions, &s->nionout, &idwn, &nidwn, &iup, &niup);
+    if (s->lecs > 0) {
+        memset(s->pind, 0, sizeof(int32_t) * s->lecs);
+        boundary_species(s, s->maxhlf, &s->lecs, &s->nlecout, &ldwn, &nldwn, &lup, &nlup);
+    }
+    /* 3D: exchange_particles + inject_others to self append the z-crossing
+       particles, first the ones that went down then up
+       (code/particles.F90:1865-2125, :1368-1421; Q8 reorder) */
+    for (int64_t n = 0; n < nidwn; n++) s->p[s->ions++] = idwn[n];
+    for (int64_t n = 0; n < nldwn; n++) s->p[s->maxhlf + s->lecs++] = ldwn[n];
+    for (int64_t n = 0; n < niup; n++) s->p[s->ions++] = iup[n];
+    for (int64_t n = 0; n < nlup; n++) s->p[s->maxhlf + s->lecs++] = lup[n];
+    free(idwn); free(iup); free(ldwn); free(lup);
+    if (s->fixed) to_fixed_to_float(s);
+}
+
+/* ------------------------------------------------------------------------
+ * Fields (code/fields.F90)
+ * --------------------------------------------------------------------- */
+void to_reset_currents(to_state *s)
+{
+    int64_t lot = to_lot(s);
+    memset(s->curx, 0, sizeof(float) * lot);
+    memset(s->cury, 0, sizeof(float) * lot);
+    memset(s->curz, 0, sizeof(float) * lot);
+    if (s->fixed) {
+        memset(s->fx, 0, sizeof(int64_t) * lot);
+        memset(s->fy, 0, sizeof(int64_t) * lot);
+        memset(s->fz, 0, sizeof(int64_t) * lot);
+    }
+}
+
+/* update ranges of advance_b_halfstep / advance_e_fullstep for one rank */
+static void b_range(const to_state *s, int axis, int *a1, int *a2)
+{
+    int m = axis == 0 ? s->mx : axis == 1 ? s->my : s->mz;
+    int ng = axis == 2 ? s->nghostz : s->nghost;
+    if (axis == 2 && s->dims == 2) { *a1 = 1; *a2 = 1; return; }
+    if (s->periodic[axis]) { *a1 = ng / 2 + 1; *a2 = m - (ng / 2 + 1); }
+    else { *a1 = 1; *a2 = m - 1; }
+}
+
+static void e_range(const to_state *s, int axis, int *a1, int *a2)
+{
+    int m = axis == 0 ? s->mx : axis == 1 ? s->my : s->mz;
+    int ng = axis == 2 ? s->nghostz : s->nghost;
+    if (axis == 2) {
+        if (s->dims == 2) { *a1 = 1; *a2 = 1; return; }
+        /* Q7: fields.F90:818-819 overrides the z range unconditionally */
+        *a1 = ng / 2;
+        *a2 = m;
+        return;
+    }
+    if (s->periodic[axis]) { *a1 = ng / 2 + 1; *a2 = m - (ng / 2 + 1); }
+    else { *a1 = ng / 2; *a2 = m; }
+}
+
+void to_advance_b_halfstep(to_state *s)
+{
+    int i1, i2, j1, j2, k1, k2;
+    b_range(s, 0, &i1, &i2);
+    b_range(s, 1, &j1, &j2);
+    b_range(s, 2, &k1, &k2);
+    const float cst = s->corr * (0.5f * s->c);
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = k1; k <= k2; k++) {
+        for (int j = j1; j <= j2; j++) {
+            for (int i = i1; i <= i2; i++) {
+                int64_t l = L3(s, i, j, k);
+                if (s->dims == 3) {
+                    s->bx[l] = s->bx[l] + cst * (s->ey[L3(s, i, j, k + 1)] - s->ey[l] - s->ez[L3(s, i, j + 1, k)] + s->ez[l]);
+                    s->by[l] = s->by[l] + cst * (s->ez[L3(s, i + 1, j, k)] - s->ez[l] - s->ex[L3(s, i, j, k + 1)] + s->ex[l]);
+                    s->bz[l] = s->bz[l] + cst * (s->ex[L3(s, i, j + 1, k)] - s->ex[l] - s->ey[L3(s, i + 1, j, k)] + s->ey[l]);
+                } else {
+                    s->bx[l] = s->bx[l] + cst * (-s->ez[L3(s, i, j + 1, k)] + s->ez[l]);
+                    s->by[l] = s->by[l] + cst * (s->ez[L3(s, i + 1, j, k)] - s->ez[l]);
+                    s->bz[l] = s->bz[l] + cst * (s->ex[L3(s, i, j + 1, k)] - s->ex[l] - s->ey[L3(s, i + 1, j, k)] + s->ey[l]);
+                }
+            }
+        }
+    }
+}
+
+void to_advance_e_fullstep(to_state *s)
+{
+    int i1, i2, j1, j2, k1, k2;
+    e_range(s, 0, &i1, &i2);
+    e_range(s, 1, &j1, &j2);
+    e_range(s, 2, &k1, &k2);
+    const float cst = s->corr * s->c;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = k1; k <= k2; k++) {
+        for (int j = j1; j <= j2; j++) {
+            for (int i = i1; i <= i2; i++) {
+                int64_t l = L3(s, i, j, k);
+                if (s->dims == 3) {
+                    s->ex[l] = s->ex[l] + cst * (s->by[L3(s, i, j, k - 1)] - s->by[l] - s->bz[L3(s, i, j - 1, k)] + s->bz[l]);
+                    s->ey[l] = s->ey[l] + cst * (s->bz[L3(s, i - 1, j, k)] - s->bz[l] - s->bx[L3(s, i, j, k - 1)] + s->bx[l]);
+                    s->ez[l] = s->ez[l] + cst * (s->bx[L3(s, i, j - 1, k)] - s->bx[l] - s->by[L3(s, i - 1, j, k)] + s->by[l]);
+                } else {
+                    s->ex[l] = s->ex[l] + cst * (-s->bz[L3(s, i, j - 1, k)] + s->bz[l]);
+                    s->ey[l] = s->ey[l] + cst * (s->bz[L3(s, i - 1, j, k)] - s->bz[l]);
+                    s->ez[l] = s->ez[l] + cst * (s->bx[L3(s, i, j - 1, k)] - s->bx[l] - s->by[L3(s, i - 1, j, k)] + s->by[l]);
+                }
+            }
+        }
+    }
+}
+
+void to_add_current(to_state *s)
+{
+    int64_t lot = to_lot(s);
+#pragma omp parallel for schedule(static)
+    for (int64_t l = 0; l < lot; l++) {
+        s->ex[l] = s->ex[l] + s->curx[l];
+        s->ey[l] = s->ey[l] + s->cury[l];
+        s->ez[l] = s->ez[l] + s->curz[l];
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Ghost layers (code/fieldboundaries.F90)
+ * copylayr{x,y} (:714-785) and copy_layrz1_opt (:1616-1680, MPI to self):
+ * layer lt <- ls over the whole face, then nt <- ns.
+ * --------------------------------------------------------------------- */
+static void copy_layer(to_state *s, float *a, int axis, int t, int src)
+{
+    int mx = s->mx, my = s->my, mz = s->mz;
+    if (axis == 0) {
+        for (int k = 1; k <= mz; k++)
+            for (int j = 1; j <= my; j++) a[L3(s, t, j, k)] = a[L3(s, src, j, k)];
+    } else if (axis == 1) {
+        for (int k = 1; k <= mz; k++)
+            for (int i = 1; i <= mx; i++) a[L3(s, i, t, k)] = a[L3(s, i, src, k)];
+    } else {
+        for (int j = 1; j <= my; j++)
+            for (int i = 1; i <= mx; i++) a[L3(s, i, j, t)] = a[L3(s, i, j, src)];
+    }
+}
+
+static void copy_layrs(to_state *s, float *a, float *b, float *c, int axis, int lt, int ls, int nt, int ns)
+{
+    copy_layer(s, a, axis, lt, ls);
+    copy_layer(s, b, axis, lt, ls);
+    copy_layer(s, c, axis, lt, ls);
+    copy_layer(s, a, axis, nt, ns);
+    copy_layer(s, b, axis, nt, ns);
+    copy_layer(s, c, axis, nt, ns);
+}
+
+static void bc_periodic(to_state *s, float *a, float *b, float *c)
+{
+    int ng = s->nghost;
+    if (s->periodic[0])
+        for (int it = 1; it <= ng / 2; it++)
+            copy_layrs(s, a, b, c, 0, ng / 2 + 1 - it, s->mx - (ng / 2 + it), s->mx - (ng / 2 + 1) + it, ng / 2 + it);
+    if (s->periodic[1])
+        for (int it = 1; it <= ng / 2; it++)
+            copy_layrs(s, a, b, c, 1, ng / 2 + 1 - it, s->my - (ng / 2 + it), s->my - (ng / 2 + 1) + it, ng / 2 + it);
+    if (s->dims == 3 && s->periodic[2]) {
+        int ngz = s->nghostz;
+        for (int it = 1; it <= ngz / 2; it++)
+            copy_layrs(s, a, b, c, 2, ngz / 2 + 1 - it, s->mz - (ngz / 2 + it), s->mz - (ngz / 2 + 1) + it, ngz / 2 + it);
+    }
+}
+
+void to_bc_b1(to_state *s) { bc_periodic(s, s->bx, s->by, s->bz); }
+void to_bc_e1(to_state *s) { bc_periodic(s, s->ex, s->ey, s->ez); }
+
+/* ------------------------------------------------------------------------
+ * Current ghost fold, exchange_current (code/fieldboundaries.F90:1768-2189)
+ * for one rank: x then y then z. Per axis and component:
+ *   cur(ng/2+1 .. ng)          += cur(m-ng/2 .. m)        (copied first)
+ *   cur(m-(ng-1) .. m-(ng/2+1)) += cur(1 .. ng/2)
+ * --------------------------------------------------------------------- */
+static void fold_axis(to_state *s, float *a, int axis, const float *q5_src)
+{
+    int m = axis == 0 ? s->mx : axis == 1 ? s->my : s->mz;
+    int ng = axis == 2 ? s->nghostz : s->nghost;
+    int n1 = axis == 0 ? s->my : s->mx;
+    int n2 = axis == 2 ? s->my : s->mz;
+    int nb1 = ng / 2 + 1, nb2 = ng / 2;
+    /* buffers hold the original source layers */
+    float *b1 = malloc(sizeof(float) * (size_t)nb1 * n1 * n2);
+    float *b2 = malloc(sizeof(float) * (size_t)nb2 * n1 * n2);
+    for (int t = 0; t < nb1; t++)
+        for (int q = 0; q < n2; q++)
+            for (int p = 0; p < n1; p++) {
+                int lay = m - ng / 2 + t;
+                int64_t l;
+                if (axis == 0) l = L3(s, lay, p + 1, q + 1);
+                else if (axis == 1) l = L3(s, p + 1, lay, q + 1);
+                else l = L3(s, p + 1, q + 1, lay);
+                float v = a[l];
+                /* Q5 (left-hand-side reading): the last buffer layer keeps
+                   what the previous component's copy left there */
+                if (q5_src && t == nb1 - 1) v = q5_src[l];
+                b1[((size_t)t * n2 + q) * n1 + p] = v;
+            }
+    for (int t = 0; t < nb2; t++)
+        for (int q = 0; q < n2; q++)
+            for (int p = 0; p < n1; p++) {
+                int lay = 1 + t;
+                int64_t l;
+                if (axis == 0) l = L3(s, lay, p + 1, q + 1);
+                else if (axis == 1) l = L3(s, p + 1, lay, q + 1);
+                else l = L3(s, p + 1, q + 1, lay);
+                b2[((size_t)t * n2 + q) * n1 + p] = a[l];
+            }
+    for (int t = 0; t < nb1; t++)
+        for (int q = 0; q < n2; q++)
+            for (int p = 0; p < n1; p++) {
+                int lay = ng / 2 + 1 + t;
+                int64_t l;
+                if (axis == 0) l = L3(s, lay, p + 1, q + 1);
+                else if (axis == 1) l = L3(s, p + 1, lay, q + 1);
+                else l = L3(s, p + 1, q + 1, lay);
+                a[l] = a[l] + b1[((size_t)t * n2 + q) * n1 + p];
+            }
+    for (int t = 0; t < nb2; t++)
+        for (int q = 0; q < n2; q++)
+            for (int p = 0; p < n1; p++) {
+                int lay = m - (ng - 1) + t;
+                int64_t l;
+                if (axis == 0) l = L3(s, lay, p + 1, q + 1);
+                else if (axis == 1) l = L3(s, p + 1, lay, q + 1);
+                else l = L3(s, p + 1, q + 1, lay);
+                a[l] = a[l] + b2[((size_t)t * n2 + q) * n1 + p];
+            }
+    free(b1);
+    free(b2);
+}
+
+void to_exchange_current(to_state *s)
+{
+    if (s->periodic[0]) {
+        fold_axis(s, s->curx, 0, NULL);
+        fold_axis(s, s->cury, 0, NULL);
+        fold_axis(s, s->curz, 0, NULL);
+    }
+    if (s->periodic[1]) {
+        fold_axis(s, s->curx, 1, NULL);
+        fold_axis(s, s->cury, 1, (s->quirks & TO_QUIRK_Q5_LHS) ? s->curx : NULL);
+        fold_axis(s, s->curz, 1, NULL);
+    }
+    if (s->dims == 3 && s->periodic[2]) {
+        fold_axis(s, s->curx, 2, NULL);
+        fold_axis(s, s->cury, 2, NULL);
+        fold_axis(s, s->curz, 2, NULL);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Binomial filter, apply_filter1_opt (code/filter.F90:8-221): ntimes
+ * passes; each refreshes one ghost layer per side (x, y, z) and applies
+ * the one-shot 9-point (2D, /16) or 27-point (3D, /64) stencil per
+ * component through `temp`. The curz row range runs two rows further
+ * (Q6, filter.F90:186,211).
+ * --------------------------------------------------------------------- */
+static void filter_component(to_state *s, float *cur, int jhi_extra)
+{
+    const int ng = s->nghost, ngz = s->nghostz;
+    const int i1 = ng / 2 + 1, i2 = s->mx - (ng / 2 + 1);
+    const int j1 = ng / 2 + 1, j2 = s->my - (ng / 2 + 1) + jhi_extra;
+    int k1 = 1, k2 = 1;
+    if (s->dims == 3) { k1 = ngz / 2 + 1; k2 = s->mz - (ngz / 2 + 1); }
+    float *temp = s->temp;
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = k1; k <= k2; k++) {
+        for (int j = j1; j <= j2; j++) {
+            for (int i = i1; i <= i2; i++) {
+#define C(a, b, cc) cur[L3(s, i + (a), j + (b), k + (cc))]
+                float t;
+                if (s->dims == 2) {
+                    const float winv = 1.0f / 16.0f;
+                    const float wtl = 2.0f * winv, wt = 4.0f * winv, wtr = 2.0f * winv, wtu = 2.0f * winv,
+                                wtb = 2.0f * winv, wtlt = 1.0f * winv, wtrt = 1.0f * winv, wtlb = 1.0f * winv,
+                                wtrb = 1.0f * winv;
+                    t = wtl * C(-1, 0, 0) + wt * C(0, 0, 0) + wtr * C(1, 0, 0) + wtb * C(0, -1, 0) +
+                        wtu * C(0, 1, 0) + wtlt * C(-1, 1, 0) + wtrt * C(1, 1, 0) + wtlb * C(-1, -1, 0) +
+                        wtrb * C(1, -1, 0);
+                } else {
+                    const float winv = 1.0f / 64.0f;
+                    const float wtl = 4.0f * winv, wt = 8.0f * winv, wtr = 4.0f * winv, wtu = 4.0f * winv,
+                                wtb = 4.0f * winv, wtlt = 2.0f * winv, wtrt = 2.0f * winv, wtlb = 2.0f * winv,
+                                wtrb = 2.0f * winv;
+                    const float wtlz = 2.0f * winv, wtz = 4.0f * winv, wtrz = 2.0f * winv, wtuz = 2.0f * winv,
+                                wtbz = 2.0f * winv, wtltz = 1.0f * winv, wtrtz = 1.0f * winv,
+                                wtlbz = 1.0f * winv, wtrbz = 1.0f * winv;
+                    t = wtl * C(-1, 0, 0) + wt * C(0, 0, 0) + wtr * C(1, 0, 0) + wtb * C(0, -1, 0) +
+                        wtu * C(0, 1, 0) + wtlt * C(-1, 1, 0) + wtrt * C(1, 1, 0) + wtlb * C(-1, -1, 0) +
+                        wtrb * C(1, -1, 0);
+                    t = t + wtlz * C(-1, 0, -1) + wtz * C(0, 0, -1) + wtrz * C(1, 0, -1) + wtbz * C(0, -1, -1) +
+                        wtuz * C(0, 1, -1) + wtltz * C(-1, 1, -1) + wtrtz * C(1, 1, -1) +
+                        wtlbz * C(-1, -1, -1) + wtrbz * C(1, -1, -1) + wtlz * C(-1, 0, 1) + wtz * C(0, 0, 1) +
+                        wtrz * C(1, 0, 1) + wtbz * C(0, -1, 1) + wtuz * C(0, 1, 1) + wtltz * C(-1, 1, 1) +
+                        wtrtz * C(1, 1, 1) + wtlbz * C(-1, -1, 1) + wtrbz * C(1, -1, 1);
+                }
+#undef C
+                temp[L3(s, i, j, k)] = t;
+            }
+        }
+    }
+#pragma omp parallel for schedule(static) collapse(2)
+    for (int k = k1; k <= k2; k++)
+        for (int j = j1; j <= j2; j++)
+            for (int i = i1; i <= i2; i++) cur[L3(s, i, j, k)] = temp[L3(s, i, j, k)];
+}
+
+void to_apply_filter1_opt(to_state *s)
+{
+    const int ng = s->nghost, ngz = s->nghostz;
+    for (int n = 1; n <= s->ntimes; n++) {
+        /* one ghost layer per side; copy_layr{x,y,z}1_opt with
+           lt=ng/2, ls=m-(ng/2+1), nt=m-ng/2, ns=ng/2+1 */
+        if (s->periodic[0])
+            copy_layrs(s, s->curx, s->cury, s->curz, 0, ng / 2, s->mx - (ng / 2 + 1), s->mx - ng / 2, ng / 2 + 1);
+        if (s->periodic[1])
+            copy_layrs(s, s->curx, s->cury, s->curz, 1, ng / 2, s->my - (ng / 2 + 1), s->my - ng / 2, ng / 2 + 1);
+        if (s->dims == 3 && s->periodic[2])
+            copy_layrs(s, s->curx, s->cury, s->curz, 2, ngz / 2, s->mz - (ngz / 2 + 1), s->mz - ngz / 2, ngz / 2 + 1);
+        filter_component(s, s->curx, 0);
+        filter_component(s, s->cury, 0);
+        filter_component(s, s->curz, 2);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Reorder (code/particles.F90:394-497): every 10 laps except the lap right
+ * after the previous reorder, stable counting sort by
+ * celli = int(x) + int(y)*iy + int(z)*iz (iz = 0 in 2D).
+ * --------------------------------------------------------------------- */
+static void reorder_range(to_state *s, int64_t base, int64_t count)
+{
+    const int64_t iy = s->mx, iz = s->dims == 3 ? (int64_t)s->mx * s->my : 0;
+    const int64_t lot = to_lot(s);
+    memset(s->pall, 0, sizeof(int32_t) * (lot + 1));
+    for (int64_t n = 0; n < count; n++) {
+        const to_particle *pp = &s->p[base + n];
+        int64_t celli = (int64_t)(int)pp->x + (int64_t)(int)pp->y * iy + (int64_t)(int)pp->z * iz;
+        if (celli < 1 || celli > lot) celli = lot; /* out of range: keep, sort last */
+        s->pall[celli]++;
+    }
+    int64_t kacc = 1;
+    for (int64_t i = 1; i <= lot; i++) {
+        int64_t j = s->pall[i];
+        s->pall[i] = (int32_t)kacc;
+        kacc += j;
+    }
+    for (int64_t n = 0; n < count; n++) {
+        const to_particle *pp = &s->p[base + n];
+        int64_t celli = (int64_t)(int)pp->x + (int64_t)(int)pp->y * iy + (int64_t)(int)pp->z * iz;
+        if (celli < 1 || celli > lot) celli = lot;
+        int64_t j = s->pall[celli];
+        s->pall[celli]++;
+        s->tempp[j - 1] = *pp;
+    }
+    memcpy(&s->p[base], s->tempp, sizeof(to_particle) * count);
+}
+
+void to_reorder_particles_(to_state *s)
+{
+    reorder_range(s, 0, s->ions);
+    reorder_range(s, s->maxhlf, s->lecs);
+}
+
+void to_reorder_particles(to_state *s)
+{
+    if (s->lap == s->lapreorder + 1) return;
+    if (s->lap % 10 != 0) return;
+    to_reorder_particles_(s);
+    s->lapreorder = s->lap;
+}
+
+/* ------------------------------------------------------------------------
+ * One lap (code/tristanmainloop.F90:107-344) for periodic boxes without
+ * radiation boundaries, injection or user particle BCs.
+ * --------------------------------------------------------------------- */
+void to_step(to_state *s)
+{
+    to_bc_b1(s);
+    to_bc_e1(s);
+    to_advance_b_halfstep(s);
+    to_bc_b1(s);
+    to_move_particles(s);
+    to_advance_b_halfstep(s);
+    to_bc_b1(s);
+    to_bc_b1(s); /* bc_b2 without radiation boundaries */
+    to_advance_e_fullstep(s);
+    to_bc_e1(s); /* bc_e2 */
+    to_reset_currents(s);
+    to_bc_e1(s);
+    to_bc_b1(s);
+    to_deposit_particles(s);
+    to_exchange_current(s);
+    to_apply_filter1_opt(s);
+    to_add_current(s);
+    to_reorder_particles(s);
+    s->lap++;
+}
+
+/* ------------------------------------------------------------------------
+ * FP64 diagnostics. rho is deposited on the interior nodes with the same
+ * B-spline (the Esirkepov deposit conserves exactly this rho), wrapped
+ * periodically, then filtered ntimes with the current filter's stencil.
+ * div E uses backward differences at nodes (E is staggered forward).
+ * --------------------------------------------------------------------- */
+static inline int wrapi(int i, int lo, int n) { return lo + ((i - lo) % n + n) % n; }
+
+void to_charge_density(const to_state *s, double *rho)
+{
+    const int ng = s->nghost, ngz = s->nghostz;
+    const int lo = ng / 2 + 1, nx = s->mx - ng, ny = s->my - ng;
+    const int loz = s->dims == 3 ? ngz / 2 + 1 : 1, nz = s->dims == 3 ? s->mz - ngz : 1;
+    const int64_t lot = to_lot(s);
+    memset(rho, 0, sizeof(double) * lot);
+    for (int sp = 0; sp < 2; sp++) {
+        int64_t base = sp == 0 ? 0 : s->maxhlf;
+        int64_t cnt = sp == 0 ? s->ions : s->lecs;
+        double qs = sp == 0 ? s->qi : s->qe;
+        for (int64_t n = 0; n < cnt; n++) {
+            const to_particle *pp = &s->p[base + n];
+            float Sx[8] = {0}, Sy[8] = {0}, Sz[8] = {0};
+            int xm, xM, ym, yM, zm = 3, zM = 3;
+            int i = (int)truncf(pp->x), j = (int)truncf(pp->y), k = (int)truncf(pp->z);
+            shape(s->order, pp->x - truncf(pp->x), Sx, 0, &xm, &xM);
+            shape(s->order, pp->y - truncf(pp->y), Sy, 0, &ym, &yM);
+            if (s->dims == 3) shape(s->order, pp->z - truncf(pp->z), Sz, 0, &zm, &zM);
+            else { Sz[3] = 1.0f; k = 1; }
+            double q = (double)pp->ch * qs;
+            for (int c = zm; c <= zM; c++)
+                for (int b = ym; b <= yM; b++)
+                    for (int a = xm; a <= xM; a++) {
+                        int ii = wrapi(i - 3 + a, lo, nx), jj = wrapi(j - 3 + b, lo, ny);
+                        int kk = s->dims == 3 ? wrapi(k - 3 + c, loz, nz) : 1;
+                        rho[L3(s, ii, jj, kk)] += q * (double)Sx[a] * (double)Sy[b] * (double)Sz[c];
+                    }
+        }
+    }
+    /* filter ntimes on the periodic interior */
+    double *tmp = malloc(sizeof(double) * lot);
+    for (int pass = 0; pass < s->ntimes; pass++) {
+        memcpy(tmp, rho, sizeof(double) * lot);
+        for (int k = loz; k < loz + nz; k++)
+            for (int j = lo; j < lo + ny; j++)
+                for (int i = lo; i < lo + nx; i++) {
+                    double acc = 0.0;
+                    for (int dc = (s->dims == 3 ? -1 : 0); dc <= (s->dims == 3 ? 1 : 0); dc++)
+                        for (int db = -1; db <= 1; db++)
+                            for (int da = -1; da <= 1; da++) {
+                                double w = (da == 0 ? 2.0 : 1.0) * (db == 0 ? 2.0 : 1.0) *
+                                           (s->dims == 3 ? (dc == 0 ? 2.0 : 1.0) : 1.0);
+                                int kk = s->dims == 3 ? wrapi(k + dc, loz, nz) : 1;
+                                acc += w * tmp[L3(s, wrapi(i + da, lo, nx), wrapi(j + db, lo, ny), kk)];
+                            }
+                    rho[L3(s, i, j, k)] = acc / (s->dims == 3 ? 64.0 : 16.0);
+                }
+    }
+    free(tmp);
+}
+
+void to_diagnostics(const to_state *s, to_diag *out)
+{
+    const int ng = s->nghost, ngz = s->nghostz;
+    const int lo = ng / 2 + 1, nx = s->mx - ng, ny = s->my - ng;
+    const int loz = s->dims == 3 ? ngz / 2 + 1 : 1, nz = s->dims == 3 ? s->mz - ngz : 1;
+    const int64_t lot = to_lot(s);
+    double *rho = malloc(sizeof(double) * lot);
+    to_charge_density(s, rho);
+    memset(out, 0, sizeof *out);
+    double r2 = 0.0, d2 = 0.0;
+    for (int k = loz; k < loz + nz; k++)
+        for (int j = lo; j < lo + ny; j++)
+            for (int i = lo; i < lo + nx; i++) {
+                int64_t l = L3(s, i, j, k);
+                double div = (double)s->ex[l] - (double)s->ex[L3(s, wrapi(i - 1, lo, nx), j, k)] +
+                             (double)s->ey[l] - (double)s->ey[L3(s, i, wrapi(j - 1, lo, ny), k)];
+                if (s->dims == 3) div += (double)s->ez[l] - (double)s->ez[L3(s, i, j, wrapi(k - 1, loz, nz))];
+                double r = div - rho[l];
+                d2 += r * r;
+                r2 += rho[l] * rho[l];
+                out->charge_total += rho[l];
+                double ex = s->ex[l], ey = s->ey[l], ez = s->ez[l], bx = s->bx[l], by = s->by[l], bz = s->bz[l];
+                out->e_field += 0.5 * (ex * ex + ey * ey + ez * ez);
+                out->e_mag += 0.5 * (bx * bx + by * by + bz * bz);
+                out->p_field[0] += ey * bz - ez * by;
+                out->p_field[1] += ez * bx - ex * bz;
+                out->p_field[2] += ex * by - ey * bx;
+            }
+    out->gauss_abs = sqrt(d2);
+    out->rho_norm = sqrt(r2);
+    out->gauss_residual = r2 > 0.0 ? sqrt(d2 / r2) : sqrt(d2);
+    for (int sp = 0; sp < 2; sp++) {
+        int64_t base = sp == 0 ? 0 : s->maxhlf;
+        int64_t cnt = sp == 0 ? s->ions : s->lecs;
+        double m = sp == 0 ? fabs((double)s->qi / (double)s->qmi) : fabs((double)s->qe / (double)s->qme);
+        double ek = 0.0;
+        for (int64_t n = 0; n < cnt; n++) {
+            const to_particle *pp = &s->p[base + n];
+            double u = pp->u, v = pp->v, w = pp->w, ch = pp->ch;
+            double gam = sqrt(1.0 + u * u + v * v + w * w);
+            ek += (gam - 1.0) * m * ch;
+            out->p_part[0] += m * ch * u;
+            out->p_part[1] += m * ch * v;
+            out->p_part[2] += m * ch * w;
+        }
+        if (sp == 0) out->e_kin_ions = ek;
+        else out->e_kin_lecs = ek;
+    }
+    free(rho);
+}

@@ -1,0 +1,116 @@
+"""Seeded synthetic initial conditions with the shapes of the reference's
+problem setups.
+
+The reference loads its plasma on the host through the user file
+(user/user_weibel.F90:252-314: two counter-streaming beams, each injected by
+inject_plasma_region with ppc0/2 per cell, code/particles.F90:2549-2938,
+Maxwell-Juttner momenta from maxwell_dist, :2176-2273, then
+reorder_particles). No dataset is involved; these loaders draw the same
+shapes from numpy's PCG64 with a fixed seed:
+
+* ion and electron of each pair share one position, uniform in the cell,
+  so the initial charge density is exactly zero (as inject_plasma_region
+  places both species of a pair at one point);
+* momenta are an isotropic non-relativistic Maxwellian of temperature
+  delgam (kT/mc^2) in the beam frame, Lorentz-boosted along +-x with the
+  beam's gamma0 (gamma0 < 1 is read as v/c, code/particles.F90:208);
+* pairs are laid out cell by cell in the reference's reorder key order
+  (x fastest), beam -x before beam +x within a cell;
+* ind counts up from 1 alternating ion / electron (inject_plasma_region's
+  ``ind=++totalpartnum``), proc = 0, splitlev = 1, ch = 1.
+
+The named workloads follow the reference's benchmark configurations: a
+128x128 order-1 Weibel box (8 per cell per species), a 1024x1024 order-3
+two-stream/Weibel box (16 per cell per species, beams at +-0.5c), a 256^3
+order-2 Weibel box (4 per cell per species, gamma0 = 5).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .config import SimConfig
+
+PARTICLE_DTYPE = np.dtype(
+    [("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("u", "<f4"), ("v", "<f4"), ("w", "<f4"),
+     ("ch", "<f4"), ("ind", "<i4"), ("proc", "<i4"), ("splitlev", "<i4")]
+)
+
+WORKLOADS = {
+    # 2D Weibel, CPU-runnable: 128^2, order 1, 8 ppc/species, gamma0 = 3
+    "weibel2d_128_o1": dict(dims=2, order=1, nx=128, ny=128, c=0.45, c_omp=10.0, ppc0=16.0,
+                            gamma0=3.0, delgam=0.01, ntimes=4),
+    # 2D two-stream/Weibel: 1024^2, order 3, 16 ppc/species, beams +-0.5c
+    "twostream2d_1024_o3": dict(dims=2, order=3, nx=1024, ny=1024, c=0.45, c_omp=10.0,
+                                ppc0=32.0, gamma0=0.5, delgam=0.005, ntimes=4),
+    # 3D Weibel: 256^3, order 2, 4 ppc/species, gamma0 = 5
+    "weibel3d_256_o2": dict(dims=3, order=2, nx=256, ny=256, nz=256, c=0.45, c_omp=8.0,
+                            ppc0=8.0, gamma0=5.0, delgam=0.01, ntimes=4),
+}
+
+
+def make_config(name: str, **overrides) -> SimConfig:
+    kw = dict(WORKLOADS[name])
+    kw.update(overrides)
+    return SimConfig(**kw)
+
+
+def load_beams(cfg: SimConfig, seed: int = 123457, ppc_species: int | None = None):
+    """Two counter-streaming pair beams filling the periodic interior.
+
+    Returns (ions, lecs) as structured arrays with the reference's particle
+    record. ``ppc_species`` defaults to ppc0/2 (both beams together).
+    """
+    rng = np.random.default_rng(seed)
+    nps = int(round(cfg.ppc0 / 2)) if ppc_species is None else int(ppc_species)
+    per_beam = max(nps // 2, 1)
+    ng, ngz = cfg.nghost, cfg.nghostz
+    x0 = ng // 2 + 1
+    nx, ny = cfg.nx, cfg.ny
+    nz = cfg.nz if cfg.dims == 3 else 1
+    ncell = nx * ny * nz
+    npairs = ncell * per_beam * 2
+    # cell origins in reorder-key order (x fastest), beam -x then +x per cell
+    cidx = np.repeat(np.arange(ncell, dtype=np.int64), per_beam * 2)
+    beam = np.tile(np.repeat(np.array([-1.0, 1.0]), per_beam), ncell)
+    ci = cidx % nx
+    cj = (cidx // nx) % ny
+    ck = cidx // (nx * ny)
+    pos = np.empty((npairs, 3), np.float32)
+    r = rng.random((npairs, 3), dtype=np.float32)
+    # keep offsets strictly below 1 after rounding to float32
+    r = np.minimum(r, np.float32(1.0 - 2.0 ** -24))
+    pos[:, 0] = (ci + x0).astype(np.float32) + r[:, 0]
+    pos[:, 1] = (cj + x0).astype(np.float32) + r[:, 1]
+    if cfg.dims == 3:
+        pos[:, 2] = (ck + (ngz // 2 + 1)).astype(np.float32) + r[:, 2]
+    else:
+        pos[:, 2] = np.float32(ngz // 2 + 1) + r[:, 2]
+    g0 = cfg.gamma_drift
+    beta0 = np.sqrt(1.0 - 1.0 / (g0 * g0))
+
+    def momenta(delgam):
+        th = rng.standard_normal((npairs, 3)) * np.sqrt(delgam)
+        gam_rest = np.sqrt(1.0 + (th * th).sum(axis=1))
+        ux = g0 * (th[:, 0] + beam * beta0 * gam_rest)
+        return np.stack([ux, th[:, 1], th[:, 2]], axis=1).astype(np.float32)
+
+    ui = momenta(cfg.delgam)
+    ue = momenta(cfg.delgam * cfg.mi / cfg.me)
+    ions = np.zeros(npairs, PARTICLE_DTYPE)
+    lecs = np.zeros(npairs, PARTICLE_DTYPE)
+    for arr, u in ((ions, ui), (lecs, ue)):
+        arr["x"], arr["y"], arr["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+        arr["u"], arr["v"], arr["w"] = u[:, 0], u[:, 1], u[:, 2]
+        arr["ch"] = 1.0
+        arr["proc"] = 0
+        arr["splitlev"] = 1
+    ids = np.arange(npairs, dtype=np.int64)
+    ions["ind"] = (2 * ids + 1).astype(np.int32)
+    lecs["ind"] = (2 * ids + 2).astype(np.int32)
+    return ions, lecs
+
+
+def with_capacity(cfg: SimConfig, nions: int, nlecs: int) -> SimConfig:
+    if cfg.maxhlf == 0:
+        cfg.maxhlf = int(max(nions, nlecs) * 1.25) + 1024
+    return cfg
