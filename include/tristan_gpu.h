@@ -1,0 +1,179 @@
+/*
+ * tristan_gpu.h -- C-ABI of the GB300 (sm_103a) TRISTAN-MP per-step hot path.
+ *
+ * Drop-in boundary for the argument-less module subroutines that the
+ * reference main loop calls each lap (mrowan137/tristan-mp-pu-master_densdecomp,
+ * code/tristanmainloop.F90:107-344). A Fortran ISO_C_BINDING shim keeps the
+ * reference's subroutine names and forwards to these entry points, so the
+ * main loop, the `input` file and the user_* hooks stay unchanged.
+ *
+ * Conventions
+ *  - Plain C types only; every call returns an int status (TG_OK = 0).
+ *  - Host arrays are the reference's own: fields are Fortran-ordered
+ *    (mx,my,mz) float arrays, particles the 40-byte `type particle` records
+ *    (code/particles.F90:51-55) with ions at p(1:ions) and electrons at
+ *    p(maxhlf+1:maxhlf+lecs).
+ *  - One context per process, one CUDA stream; calls are stream-ordered and
+ *    return without a host synchronisation except tg_sync_to_host,
+ *    tg_synchronize, tg_diag_fp64 and tg_get_counts. A context is not
+ *    thread-safe.
+ *  - Device-side faults (a particle outside the grid, a NaN, a capacity
+ *    overflow) are recorded in a device status word, never trapped; the next
+ *    synchronising call returns the matching TG_ERR_* code and
+ *    tg_last_error() describes it.
+ */
+#ifndef TRISTAN_GPU_H
+#define TRISTAN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_OK 0
+#define TG_ERR_ARG 1      /* bad argument or configuration */
+#define TG_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define TG_ERR_OVERFLOW 3 /* particle count above maxhlf (check_overflow,
+                             code/particles.F90:362-370) */
+#define TG_ERR_BOUNDS 4   /* a particle or deposit left the local grid */
+#define TG_ERR_NAN 5      /* non-finite particle coordinate */
+#define TG_ERR_STATE 6    /* call made in the wrong order (e.g. unbound) */
+
+/* quirk switches, tg_config.quirks */
+#define TG_QUIRK_Q5_LHS 1 /* y-fold of cury reads curx(:,my) for row nghost,
+                             the left-hand-side reading of the shape-mismatched
+                             copy at code/fieldboundaries.F90:1938 */
+
+/* deposit modes, tg_config.deposit_mode */
+#define TG_DEPOSIT_FP32 0  /* FP32 shared-memory atomics, reference arithmetic */
+#define TG_DEPOSIT_FIXED 1 /* int64 fixed point: bit-reproducible currents */
+
+/* sync masks */
+#define TG_SYNC_E 1u
+#define TG_SYNC_B 2u
+#define TG_SYNC_CUR 4u
+#define TG_SYNC_PARTICLES 8u
+#define TG_SYNC_ALL 15u
+
+/* Run configuration: the values the reference reads from `input` and
+   derives at start-up (read_input_grid code/fields.F90:154-192,
+   allocate_fields :207-360, read_input_particles code/particles.F90:189-233,
+   allocate_particles :286-341, read_input_algorithm
+   code/initialize.F90:293-305). */
+typedef struct {
+    int32_t dims;        /* 2 (twoD build) or 3 */
+    int32_t order;       /* shape order 1, 2, 3 (-Ddd1/-Ddd2/-Ddd3) */
+    int32_t mx, my, mz;  /* local extents including ghosts; 2D: mz = 1 */
+    int32_t nghost, nghostz;
+    int32_t periodic[3];
+    int32_t ntimes;      /* filter passes */
+    int32_t quirks;
+    float c, corr;
+    float qi, qe, qmi, qme;
+    int32_t external_fields; /* add ext[] in the mover (get_external_fields) */
+    float ext[6];            /* ex, ey, ez, bx, by, bz */
+    double x1in, x2in, y1in, y2in, z1in, z2in; /* keep-window on open axes */
+    int64_t mxcum, mycum, mzcum;               /* slab offsets (0 for one domain) */
+    int32_t deposit_mode;
+    int32_t fx_shift;    /* fixed-point scale 2^fx_shift */
+    int64_t maxhlf;      /* particle capacity per species */
+    int32_t sort_every;  /* re-sort particles into tiles every k laps (>= 1) */
+    int32_t tile[3];     /* tile edge in cells (0 = automatic) */
+    int32_t device;      /* CUDA device ordinal */
+} tg_config;
+
+typedef struct tg_ctx tg_ctx;
+
+/* FP64 diagnostics (reduced on the device) */
+typedef struct {
+    double gauss_residual; /* ||div E - F^ntimes(rho)|| / ||F^ntimes(rho)|| */
+    double gauss_abs;
+    double rho_norm;
+    double e_field, e_mag;      /* sum E^2/2, sum B^2/2 over the interior */
+    double e_kin_ions, e_kin_lecs;
+    double p_part[3];           /* sum m u */
+    double p_field[3];          /* sum E x B */
+    double charge_total;
+} tg_diag;
+
+/* Allocate the device domain: replaces allocate_fields
+   (code/fields.F90:207-360) and allocate_particles
+   (code/particles.F90:286-341). */
+int tg_init(const tg_config *cfg, tg_ctx **out);
+/* Release everything (finalize, code/tristan.F90:38). */
+void tg_finalize(tg_ctx *ctx);
+/* Text of the last error on this context (or of the last failed tg_init
+   when ctx is NULL). */
+const char *tg_last_error(tg_ctx *ctx);
+
+/* Register the host Fortran arrays (module m_fields, code/fields.F90:81-86).
+   Any pointer may be NULL. */
+int tg_bind_fields(tg_ctx *ctx, float *ex, float *ey, float *ez, float *bx, float *by,
+                   float *bz, float *curx, float *cury, float *curz);
+/* Register the host particle array p (2*maxhlf records) and the species
+   counters ions/lecs (module m_particles, code/particles.F90:80-100). */
+int tg_bind_particles(tg_ctx *ctx, void *p, int32_t *ions, int32_t *lecs);
+/* Host -> device for the masked groups (after host-side injection or
+   field_bc_user edits). Particles are sorted into tiles on upload. */
+int tg_sync_from_host(tg_ctx *ctx, unsigned mask);
+/* Device -> host for the masked groups (before Diagnostics, output,
+   restart, host-side user hooks). Synchronises. */
+int tg_sync_to_host(tg_ctx *ctx, unsigned mask);
+
+/* bc_b1 / bc_e1: periodic ghost-layer copies (code/fieldboundaries.F90:
+   181-263, :306-392). bc_b2 / bc_e2 reduce to these without radiation
+   boundaries. */
+int tg_bc_b1(tg_ctx *ctx);
+int tg_bc_e1(tg_ctx *ctx);
+/* advance_Bhalfstep (code/fields.F90:1407-1415 -> advance_b_halfstep
+   :586-728): B += corr*c/2 * (-curl E) on the update range. */
+int tg_advance_b_half(tg_ctx *ctx);
+/* advance_Efield (code/fields.F90:1425-1433 -> advance_e_fullstep
+   :739-870): E += corr*c * curl B. */
+int tg_advance_e(tg_ctx *ctx);
+/* move_particles (code/particles_movedeposit.F90:63-88): Boris push with
+   the shape-consistent gather, both species. */
+int tg_move(tg_ctx *ctx);
+/* reset_currents (code/fields.F90:499-506). */
+int tg_reset_currents(tg_ctx *ctx);
+/* deposit_particles (code/particles_movedeposit.F90:1281-2051): Esirkepov
+   current of every particle from its reconstructed previous position, then
+   the periodic wrap / open-boundary discard and compaction. */
+int tg_deposit(tg_ctx *ctx);
+/* exchange_current (code/fieldboundaries.F90:1768-2189): fold the current
+   ghost layers into the interior. */
+int tg_fold_currents(tg_ctx *ctx);
+/* apply_filter1_opt (code/filter.F90:8-221): ntimes binomial passes. */
+int tg_filter(tg_ctx *ctx);
+/* add_current (code/fields.F90:1372-1395): E += cur over the array. */
+int tg_add_current(tg_ctx *ctx);
+/* reorder_particles (code/particles.F90:394-403): stable counting sort of
+   each species by cell, on the reference's cadence (every 10 laps, not the
+   lap after the previous reorder). force != 0 sorts now. */
+int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force);
+
+/* One or more complete laps of the periodic main loop
+   (code/tristanmainloop.F90:115-303 without output, injection and domain
+   moves), fused and replayed from a captured CUDA graph. */
+int tg_step(tg_ctx *ctx, int32_t nsteps);
+/* FP64 Gauss-law residual, energies and momenta of the device state.
+   Synchronises. */
+int tg_diag_fp64(tg_ctx *ctx, tg_diag *out);
+
+/* Wait for all work on the context's stream; returns any device status. */
+int tg_synchronize(tg_ctx *ctx);
+/* Current particle counts per species (synchronises). */
+int tg_get_counts(tg_ctx *ctx, int64_t *ions, int64_t *lecs);
+/* Raw device pointers of the field arrays in the order ex, ey, ez, bx, by,
+   bz, curx, cury, curz (for zero-copy coupling; valid until tg_finalize). */
+int tg_device_fields(tg_ctx *ctx, float **ptrs9);
+/* The CUDA stream the context launches on (as a cudaStream_t). */
+void *tg_stream(tg_ctx *ctx);
+/* Number of kernels launched by the last tg_step lap (for accounting). */
+int32_t tg_kernels_per_step(tg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

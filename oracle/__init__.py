@@ -37,6 +37,12 @@ PARTICLE_DTYPE = np.dtype(
 def build(force: bool = False) -> None:
     """Compile the serial (parity) and OpenMP (CPU baseline) oracle libraries."""
     os.makedirs(BUILD, exist_ok=True)
+    import platform
+    stamp = os.path.join(BUILD, "host_arch")
+    if not os.path.exists(stamp) or open(stamp).read().strip() != platform.machine():
+        force = True
+        with open(stamp, "w") as fh:
+            fh.write(platform.machine() + "\n")
     common = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=c11",
               "-Wall", "-Wno-unused-variable", "-Wno-unused-but-set-variable", "-Wno-unknown-pragmas"]
     jobs = []

@@ -1,0 +1,697 @@
+// C-ABI of the GB300 TRISTAN-MP hot path: context, device memory, the
+// per-subroutine entry points and the fused, graph-captured lap.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "tg_internal.cuh"
+
+using namespace tg;
+
+static thread_local char g_init_error[512];
+
+struct tg_ctx {
+    tg_config cfg;
+    Geom g;
+    Params P;
+    cudaStream_t st = nullptr;
+    int device = 0;
+    // device fields: ex ey ez bx by bz curx cury curz
+    float *f[9] = {};
+    float *ftmp[3] = {};   // filter ping-pong
+    float *prim[6] = {};   // 3D primal copies
+    unsigned long long *fix[3] = {};
+    // particles: [parity][species]
+    Species sp[2][2];
+    int par = 0;
+    long long *d_cnt = nullptr;  // [parity][species]
+    long long hcount[2] = {0, 0};
+    int *tstart[2] = {}, *hist[2] = {}, *cursor[2] = {};
+    int *d_status = nullptr;
+    bool dirty = true;      // particles not grouped by tile
+    // host bindings
+    float *hf[9] = {};
+    void *hp = nullptr;
+    int32_t *hions = nullptr, *hlecs = nullptr;
+    // staging / scratch
+    void *stage = nullptr;
+    int *rk[4] = {};        // reorder keys in/out, values in/out
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    // graphs: one cycle of 2*sort_every laps per starting parity
+    cudaGraphExec_t cycle[2] = {nullptr, nullptr};
+    int kernels_per_step = 0;
+    long long lap = 0;
+    long long lapreorder = 0;
+    char err[512] = {0};
+    std::vector<void *> allocs;
+};
+
+static int fail(tg_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) snprintf(c->err, sizeof c->err, "%s", buf);
+    else snprintf(g_init_error, sizeof g_init_error, "%s", buf);
+    return code;
+}
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e__ = (call);                                                                \
+        if (e__ != cudaSuccess)                                                                  \
+            return fail(ctx, TG_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e__), \
+                        __FILE__, __LINE__);                                                     \
+    } while (0)
+
+template <class T>
+static int dalloc(tg_ctx *ctx, T **p, size_t n) {
+    void *q = nullptr;
+    CK(cudaMalloc(&q, n * sizeof(T) + 256));
+    ctx->allocs.push_back(q);
+    *p = (T *)q;
+    return TG_OK;
+}
+
+static int check_status(tg_ctx *ctx) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (st == 0) return TG_OK;
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->st));
+    if (st & ST_NAN) return fail(ctx, TG_ERR_NAN, "non-finite particle coordinate (device status %d)", st);
+    if (st & ST_OVERFLOW) return fail(ctx, TG_ERR_OVERFLOW, "particle capacity exceeded (device status %d)", st);
+    return fail(ctx, TG_ERR_BOUNDS, "particle or deposit outside the local grid (device status %d)", st);
+}
+
+// ---------------------------------------------------------------------------
+// geometry
+// ---------------------------------------------------------------------------
+static int setup_geom(tg_ctx *ctx) {
+    const tg_config &c = ctx->cfg;
+    Geom &g = ctx->g;
+    memset(&g, 0, sizeof g);
+    if (c.dims != 2 && c.dims != 3) return fail(ctx, TG_ERR_ARG, "dims must be 2 or 3 (got %d)", c.dims);
+    if (c.order < 1 || c.order > 3) return fail(ctx, TG_ERR_ARG, "order must be 1, 2 or 3 (got %d)", c.order);
+    const int ng_expect = c.order == 1 ? 5 : 7;
+    if (c.nghost != ng_expect)
+        return fail(ctx, TG_ERR_ARG, "nghost must be %d for order %d (got %d)", ng_expect, c.order, c.nghost);
+    if (c.dims == 2 && (c.mz != 1 || c.nghostz != 5))
+        return fail(ctx, TG_ERR_ARG, "2D needs mz = 1 and nghostz = 5");
+    if (c.dims == 3 && c.nghostz != c.nghost) return fail(ctx, TG_ERR_ARG, "3D needs nghostz = nghost");
+    g.dims = c.dims;
+    g.order = c.order;
+    g.mx = c.mx;
+    g.my = c.my;
+    g.mz = c.mz;
+    g.ng = c.nghost;
+    g.ngz = c.nghostz;
+    const int nx = c.mx - g.ng, ny = c.my - g.ng, nz = c.dims == 3 ? c.mz - g.ngz : 1;
+    if (nx < 4 || ny < 4 || nz < 1 || (c.dims == 3 && nz < 4))
+        return fail(ctx, TG_ERR_ARG, "grid too small (%d x %d x %d interior cells)", nx, ny, nz);
+    g.lot = (long long)c.mx * c.my * c.mz;
+    if (g.lot >= (1LL << 31)) return fail(ctx, TG_ERR_ARG, "grid of %lld cells exceeds int32 cell indices", g.lot);
+    g.sy = c.mx;
+    g.sz = (long long)c.mx * c.my;
+    for (int a = 0; a < 3; a++) g.per[a] = c.periodic[a] ? 1 : 0;
+    if (c.dims == 2) g.per[2] = 0;
+    g.minx = (float)(g.ng / 2 + 1);
+    g.maxx = (float)c.mx - 1.0f * (float)(g.ng / 2);
+    g.miny = (float)(g.ng / 2 + 1);
+    g.maxy = (float)c.my - 1.0f * (float)(g.ng / 2);
+    if (c.dims == 3) {
+        g.minz = 1.0f * (float)(g.ngz / 2 + 1);
+        g.maxz = (float)c.mz - 1.0f * (float)(g.ngz / 2);
+    } else {
+        g.minz = 1.0f * (float)(g.ngz / 2 + 1);
+        g.maxz = 1.0f * (float)(g.ngz / 2 + 1) + 1.0f;
+    }
+    // tiles
+    int tx = c.tile[0], ty = c.tile[1], tz = c.tile[2];
+    if (tx <= 0) tx = c.dims == 3 ? 8 : 16;
+    if (ty <= 0) ty = c.dims == 3 ? 8 : 16;
+    if (tz <= 0) tz = c.dims == 3 ? 8 : 1;
+    if (c.dims == 2) tz = 1;
+    g.tx = tx;
+    g.ty = ty;
+    g.tz = tz;
+    g.ox = g.ng / 2 + 1;
+    g.oy = g.ng / 2 + 1;
+    g.oz = c.dims == 3 ? g.ngz / 2 + 1 : 1;
+    g.ntx = (nx + tx - 1) / tx;
+    g.nty = (ny + ty - 1) / ty;
+    g.ntz = c.dims == 3 ? (nz + tz - 1) / tz : 1;
+    g.ntiles = g.ntx * g.nty * g.ntz;
+    const int se = c.sort_every < 1 ? 1 : c.sort_every;
+    const int drift = 1 + (int)ceilf((float)(se - 1) * c.c);
+    g.wlo = 2 + drift;
+    g.whi = 3 + drift;
+    g.wx = tx + g.wlo + g.whi;
+    g.wy = ty + g.wlo + g.whi;
+    g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
+    g.wcells = g.wx * g.wy * g.wz;
+    const size_t smem = (size_t)3 * g.wcells * (c.deposit_mode == TG_DEPOSIT_FIXED ? 8 : 4);
+    if (smem > 227 * 1024)
+        return fail(ctx, TG_ERR_ARG, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
+    return TG_OK;
+}
+
+static void setup_params(tg_ctx *ctx) {
+    const tg_config &c = ctx->cfg;
+    Params &P = ctx->P;
+    memset(&P, 0, sizeof P);
+    P.c = c.c;
+    P.corr = c.corr;
+    P.qm[0] = c.qmi;
+    P.qm[1] = c.qme;
+    P.qs[0] = c.qi;
+    P.qs[1] = c.qe;
+    P.external_fields = c.external_fields;
+    for (int a = 0; a < 6; a++) P.ext[a] = c.ext[a];
+    P.x1in = c.x1in; P.x2in = c.x2in; P.y1in = c.y1in; P.y2in = c.y2in; P.z1in = c.z1in; P.z2in = c.z2in;
+    P.mxcum = c.mxcum; P.mycum = c.mycum; P.mzcum = c.mzcum;
+    P.fixed = c.deposit_mode == TG_DEPOSIT_FIXED;
+    P.fx_scale = ldexpf(1.0f, c.fx_shift);
+    P.fx_inv = ldexp(1.0, -c.fx_shift);
+    P.quirks = c.quirks;
+}
+
+static int alloc_species(tg_ctx *ctx, Species &s, size_t n) {
+    int r;
+    if ((r = dalloc(ctx, &s.cell, n))) return r;
+    if ((r = dalloc(ctx, &s.ox, n))) return r;
+    if ((r = dalloc(ctx, &s.oy, n))) return r;
+    if ((r = dalloc(ctx, &s.oz, n))) return r;
+    if ((r = dalloc(ctx, &s.u, n))) return r;
+    if ((r = dalloc(ctx, &s.v, n))) return r;
+    if ((r = dalloc(ctx, &s.w, n))) return r;
+    if ((r = dalloc(ctx, &s.ch, n))) return r;
+    if ((r = dalloc(ctx, &s.ind, n))) return r;
+    if ((r = dalloc(ctx, &s.proc, n))) return r;
+    if ((r = dalloc(ctx, &s.splitlev, n))) return r;
+    return TG_OK;
+}
+
+extern "C" int tg_init(const tg_config *cfg, tg_ctx **out) {
+    if (!cfg || !out) return fail(nullptr, TG_ERR_ARG, "tg_init: null argument");
+    *out = nullptr;
+    tg_ctx *ctx = new (std::nothrow) tg_ctx();
+    if (!ctx) return fail(nullptr, TG_ERR_ARG, "tg_init: out of host memory");
+    ctx->cfg = *cfg;
+    int r = setup_geom(ctx);
+    if (r) {
+        fail(nullptr, r, "%s", ctx->err);
+        delete ctx;
+        return r;
+    }
+    setup_params(ctx);
+    if (cfg->maxhlf <= 0 || cfg->maxhlf >= (1LL << 31)) {
+        delete ctx;
+        return fail(nullptr, TG_ERR_ARG, "maxhlf must be in [1, 2^31)");
+    }
+    ctx->device = cfg->device;
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        fail(nullptr, TG_ERR_CUDA, "tg_init: CUDA device %d unavailable: %s", cfg->device, cudaGetErrorString(e));
+        delete ctx;
+        return TG_ERR_CUDA;
+    }
+    const Geom &g = ctx->g;
+    const size_t lot = (size_t)g.lot;
+    r = TG_OK;
+    for (int a = 0; a < 9 && !r; a++) r = dalloc(ctx, &ctx->f[a], lot);
+    for (int a = 0; a < 3 && !r; a++) r = dalloc(ctx, &ctx->ftmp[a], lot);
+    if (g.dims == 3)
+        for (int a = 0; a < 6 && !r; a++) r = dalloc(ctx, &ctx->prim[a], lot);
+    if (ctx->P.fixed)
+        for (int a = 0; a < 3 && !r; a++) r = dalloc(ctx, &ctx->fix[a], lot);
+    for (int p = 0; p < 2 && !r; p++)
+        for (int s = 0; s < 2 && !r; s++) r = alloc_species(ctx, ctx->sp[p][s], (size_t)cfg->maxhlf);
+    if (!r) r = dalloc(ctx, &ctx->d_cnt, 4);
+    for (int s = 0; s < 2 && !r; s++) {
+        r = dalloc(ctx, &ctx->tstart[s], (size_t)g.ntiles + 1);
+        if (!r) r = dalloc(ctx, &ctx->hist[s], (size_t)g.ntiles);
+        if (!r) r = dalloc(ctx, &ctx->cursor[s], (size_t)g.ntiles);
+    }
+    if (!r) r = dalloc(ctx, &ctx->d_status, 1);
+    if (r) {
+        snprintf(g_init_error, sizeof g_init_error, "%s", ctx->err);
+        tg_finalize(ctx);
+        return r;
+    }
+    cudaStream_t st = ctx->st;
+    for (int a = 0; a < 9; a++) e = e != cudaSuccess ? e : cudaMemsetAsync(ctx->f[a], 0, lot * 4, st);
+    for (int a = 0; a < 3; a++) e = e != cudaSuccess ? e : cudaMemsetAsync(ctx->ftmp[a], 0, lot * 4, st);
+    if (ctx->P.fixed)
+        for (int a = 0; a < 3; a++) e = e != cudaSuccess ? e : cudaMemsetAsync(ctx->fix[a], 0, lot * 8, st);
+    for (int s = 0; s < 2; s++) {
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->tstart[s], 0, ((size_t)g.ntiles + 1) * 4, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->hist[s], 0, (size_t)g.ntiles * 4, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->cursor[s], 0, (size_t)g.ntiles * 4, st);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_cnt, 0, 4 * sizeof(long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        fail(nullptr, TG_ERR_CUDA, "tg_init: %s", cudaGetErrorString(e));
+        tg_finalize(ctx);
+        return TG_ERR_CUDA;
+    }
+    *out = ctx;
+    return TG_OK;
+}
+
+extern "C" void tg_finalize(tg_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (int p = 0; p < 2; p++)
+        if (ctx->cycle[p]) cudaGraphExecDestroy(ctx->cycle[p]);
+    for (void *q : ctx->allocs) cudaFree(q);
+    if (ctx->stage) cudaFree(ctx->stage);
+    for (int a = 0; a < 4; a++)
+        if (ctx->rk[a]) cudaFree(ctx->rk[a]);
+    if (ctx->cub_tmp) cudaFree(ctx->cub_tmp);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+extern "C" const char *tg_last_error(tg_ctx *ctx) { return ctx ? ctx->err : g_init_error; }
+
+extern "C" int tg_synchronize(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_status(ctx);
+}
+
+extern "C" void *tg_stream(tg_ctx *ctx) { return ctx ? (void *)ctx->st : nullptr; }
+
+extern "C" int tg_device_fields(tg_ctx *ctx, float **ptrs9) {
+    if (!ctx || !ptrs9) return TG_ERR_ARG;
+    for (int a = 0; a < 9; a++) ptrs9[a] = ctx->f[a];
+    return TG_OK;
+}
+
+extern "C" int32_t tg_kernels_per_step(tg_ctx *ctx) { return ctx ? ctx->kernels_per_step : 0; }
+
+// ---------------------------------------------------------------------------
+// tile sort: count (unless the tile kernel already did), scan, scatter,
+// flip parity
+// ---------------------------------------------------------------------------
+static int sort_species(tg_ctx *ctx, int s, bool counted) {
+    const int p = ctx->par;
+    long long *cnt_cur = ctx->d_cnt + 2 * p + s, *cnt_next = ctx->d_cnt + 2 * (1 - p) + s;
+    if (!counted) CK(launch_tile_count(ctx->g, ctx->sp[p][s], cnt_cur, ctx->hcount[s], ctx->hist[s], ctx->st));
+    CK(launch_scan(ctx->hist[s], ctx->tstart[s], ctx->cursor[s], ctx->g.ntiles, cnt_next, ctx->st));
+    CK(launch_scatter(ctx->g, ctx->sp[p][s], ctx->sp[1 - p][s], cnt_cur, ctx->hcount[s], ctx->tstart[s],
+                      ctx->cursor[s], ctx->st));
+    return TG_OK;
+}
+
+static int sort_all(tg_ctx *ctx, bool counted) {
+    int r;
+    if ((r = sort_species(ctx, 0, counted))) return r;
+    if ((r = sort_species(ctx, 1, counted))) return r;
+    ctx->par ^= 1;
+    ctx->dirty = false;
+    return TG_OK;
+}
+
+static int ensure_sorted(tg_ctx *ctx) {
+    if (!ctx->dirty) return TG_OK;
+    return sort_all(ctx, false);
+}
+
+static TileArgs tile_args(tg_ctx *ctx, bool count_tiles) {
+    TileArgs a;
+    memset(&a, 0, sizeof a);
+    a.g = ctx->g;
+    a.P = ctx->P;
+    a.f.ex = ctx->f[0]; a.f.ey = ctx->f[1]; a.f.ez = ctx->f[2];
+    a.f.bx = ctx->f[3]; a.f.by = ctx->f[4]; a.f.bz = ctx->f[5];
+    a.f.pex = ctx->prim[0]; a.f.pey = ctx->prim[1]; a.f.pez = ctx->prim[2];
+    a.f.pbx = ctx->prim[3]; a.f.pby = ctx->prim[4]; a.f.pbz = ctx->prim[5];
+    for (int s = 0; s < 2; s++) {
+        a.sp[s] = ctx->sp[ctx->par][s];
+        a.tstart[s] = ctx->tstart[s];
+        a.newcount[s] = count_tiles ? ctx->hist[s] : nullptr;
+    }
+    for (int cc = 0; cc < 3; cc++) {
+        a.cur[cc] = ctx->f[6 + cc];
+        a.fix[cc] = ctx->fix[cc];
+    }
+    a.status = ctx->d_status;
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// bindings and host transfers
+// ---------------------------------------------------------------------------
+extern "C" int tg_bind_fields(tg_ctx *ctx, float *ex, float *ey, float *ez, float *bx, float *by, float *bz,
+                              float *curx, float *cury, float *curz) {
+    if (!ctx) return TG_ERR_ARG;
+    float *h[9] = {ex, ey, ez, bx, by, bz, curx, cury, curz};
+    for (int a = 0; a < 9; a++) ctx->hf[a] = h[a];
+    return TG_OK;
+}
+
+extern "C" int tg_bind_particles(tg_ctx *ctx, void *p, int32_t *ions, int32_t *lecs) {
+    if (!ctx || !p || !ions || !lecs) return fail(ctx, TG_ERR_ARG, "tg_bind_particles: null argument");
+    ctx->hp = p;
+    ctx->hions = ions;
+    ctx->hlecs = lecs;
+    return TG_OK;
+}
+
+static const size_t AOS = 40;
+
+extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
+    if (!ctx) return TG_ERR_ARG;
+    const size_t lot = (size_t)ctx->g.lot;
+    const int groups[3][4] = {{0, 1, 2, (int)TG_SYNC_E}, {3, 4, 5, (int)TG_SYNC_B}, {6, 7, 8, (int)TG_SYNC_CUR}};
+    for (int gi = 0; gi < 3; gi++) {
+        if (!(mask & (unsigned)groups[gi][3])) continue;
+        for (int a = 0; a < 3; a++) {
+            float *h = ctx->hf[groups[gi][a]];
+            if (!h) return fail(ctx, TG_ERR_STATE, "tg_sync_from_host: field array %d not bound", groups[gi][a]);
+            CK(cudaMemcpyAsync(ctx->f[groups[gi][a]], h, lot * 4, cudaMemcpyHostToDevice, ctx->st));
+        }
+    }
+    if (mask & TG_SYNC_PARTICLES) {
+        if (!ctx->hp) return fail(ctx, TG_ERR_STATE, "tg_sync_from_host: particles not bound");
+        const long long n[2] = {*ctx->hions, *ctx->hlecs};
+        for (int s = 0; s < 2; s++)
+            if (n[s] < 0 || n[s] > ctx->cfg.maxhlf)
+                return fail(ctx, TG_ERR_OVERFLOW, "species %d count %lld outside [0, maxhlf=%lld]", s, n[s],
+                            (long long)ctx->cfg.maxhlf);
+        if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+        for (int s = 0; s < 2; s++) {
+            const char *src = (const char *)ctx->hp + (s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS);
+            CK(cudaMemcpyAsync(ctx->stage, src, (size_t)n[s] * AOS, cudaMemcpyHostToDevice, ctx->st));
+            CK(launch_aos_to_soa(ctx->g, ctx->stage, ctx->sp[ctx->par][s], n[s], ctx->d_status, ctx->st));
+            CK(cudaMemcpyAsync(ctx->d_cnt + 2 * ctx->par + s, &n[s], sizeof(long long), cudaMemcpyHostToDevice,
+                               ctx->st));
+            ctx->hcount[s] = n[s];
+        }
+        CK(cudaStreamSynchronize(ctx->st));  // n[] lives on this stack frame
+        ctx->dirty = true;
+    }
+    return TG_OK;
+}
+
+// current counts of the buffer in use (drops discarded particles first)
+static int exact_counts(tg_ctx *ctx, long long n[2]) {
+    int r = ensure_sorted(ctx);
+    if (r) return r;
+    CK(cudaMemcpyAsync(n, ctx->d_cnt + 2 * ctx->par, 2 * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->hcount[0] = n[0];
+    ctx->hcount[1] = n[1];
+    return TG_OK;
+}
+
+extern "C" int tg_get_counts(tg_ctx *ctx, int64_t *ions, int64_t *lecs) {
+    if (!ctx) return TG_ERR_ARG;
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    if (ions) *ions = n[0];
+    if (lecs) *lecs = n[1];
+    return check_status(ctx);
+}
+
+extern "C" int tg_sync_to_host(tg_ctx *ctx, unsigned mask) {
+    if (!ctx) return TG_ERR_ARG;
+    const size_t lot = (size_t)ctx->g.lot;
+    const int groups[3][4] = {{0, 1, 2, (int)TG_SYNC_E}, {3, 4, 5, (int)TG_SYNC_B}, {6, 7, 8, (int)TG_SYNC_CUR}};
+    for (int gi = 0; gi < 3; gi++) {
+        if (!(mask & (unsigned)groups[gi][3])) continue;
+        for (int a = 0; a < 3; a++) {
+            float *h = ctx->hf[groups[gi][a]];
+            if (!h) return fail(ctx, TG_ERR_STATE, "tg_sync_to_host: field array %d not bound", groups[gi][a]);
+            CK(cudaMemcpyAsync(h, ctx->f[groups[gi][a]], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
+        }
+    }
+    if (mask & TG_SYNC_PARTICLES) {
+        if (!ctx->hp) return fail(ctx, TG_ERR_STATE, "tg_sync_to_host: particles not bound");
+        long long n[2];
+        int r = exact_counts(ctx, n);
+        if (r) return r;
+        if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+        for (int s = 0; s < 2; s++) {
+            char *dst = (char *)ctx->hp + (s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS);
+            CK(launch_soa_to_aos(ctx->g, ctx->sp[ctx->par][s], ctx->stage, n[s], ctx->st));
+            CK(cudaMemcpyAsync(dst, ctx->stage, (size_t)n[s] * AOS, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
+        }
+        *ctx->hions = (int32_t)n[0];
+        *ctx->hlecs = (int32_t)n[1];
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// per-subroutine entry points
+// ---------------------------------------------------------------------------
+extern "C" int tg_bc_b1(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_ghost(ctx->g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_bc_e1(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_ghost(ctx->g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_advance_b_half(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_advance_b(ctx->g, ctx->P, ctx->f, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_advance_e(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_advance_e(ctx->g, ctx->P, ctx->f, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_move(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    FieldPtrs fp;
+    fp.ex = ctx->f[0]; fp.ey = ctx->f[1]; fp.ez = ctx->f[2];
+    fp.bx = ctx->f[3]; fp.by = ctx->f[4]; fp.bz = ctx->f[5];
+    fp.pex = ctx->prim[0]; fp.pey = ctx->prim[1]; fp.pez = ctx->prim[2];
+    fp.pbx = ctx->prim[3]; fp.pby = ctx->prim[4]; fp.pbz = ctx->prim[5];
+    if (ctx->g.dims == 3) CK(launch_primal(ctx->g, ctx->f, ctx->prim, ctx->st));
+    for (int s = 0; s < 2; s++)
+        CK(launch_push_flat(ctx->g, ctx->P, fp, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,
+                            ctx->hcount[s], ctx->P.qm[s], ctx->d_status, ctx->st));
+    ctx->dirty = true;
+    return TG_OK;
+}
+
+extern "C" int tg_reset_currents(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    const size_t lot = (size_t)ctx->g.lot;
+    for (int a = 6; a < 9; a++) CK(cudaMemsetAsync(ctx->f[a], 0, lot * 4, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_deposit(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    int r = ensure_sorted(ctx);
+    if (r) return r;
+    TileArgs a = tile_args(ctx, false);
+    CK(launch_tiles(a, ctx->P.fixed != 0, false, true, ctx->st));
+    if (ctx->P.fixed) {
+        // cur = the fixed-point sum since reset_currents (which it follows)
+        float *cur3[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
+        CK(launch_fixed_to_float(ctx->g, ctx->P, ctx->fix, cur3, ctx->st));
+    }
+    ctx->dirty = true;  // wrapped particles left their tiles
+    return TG_OK;
+}
+
+extern "C" int tg_fold_currents(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_fold(ctx->g, ctx->P, ctx->f + 6, ctx->st));
+    return TG_OK;
+}
+
+static int filter_passes(tg_ctx *ctx) {
+    float *a[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
+    float *b[3] = {ctx->ftmp[0], ctx->ftmp[1], ctx->ftmp[2]};
+    for (int n = 0; n < ctx->cfg.ntimes; n++) {
+        if (n % 2 == 0) CK(launch_filter_pass(ctx->g, a, b, ctx->st));
+        else CK(launch_filter_pass(ctx->g, b, a, ctx->st));
+    }
+    if (ctx->cfg.ntimes % 2 == 1)
+        for (int cc = 0; cc < 3; cc++)
+            CK(cudaMemcpyAsync(a[cc], b[cc], (size_t)ctx->g.lot * 4, cudaMemcpyDeviceToDevice, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_filter(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    return filter_passes(ctx);
+}
+
+extern "C" int tg_add_current(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(launch_add_current(ctx->g, ctx->f, ctx->st));
+    return TG_OK;
+}
+
+extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!force) {
+        // code/particles.F90:398-400
+        if (lap == ctx->lapreorder + 1) return TG_OK;
+        if (lap % 10 != 0) return TG_OK;
+    }
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    const size_t cap = (size_t)ctx->cfg.maxhlf;
+    for (int a = 0; a < 4; a++)
+        if (!ctx->rk[a]) CK(cudaMalloc(&ctx->rk[a], cap * 4 + 256));
+    const long long maxkey = (long long)ctx->g.lot + ctx->g.sy + ctx->g.sz + ctx->g.mx + 1;
+    int end_bit = 1;
+    while ((1LL << end_bit) <= maxkey) end_bit++;
+    if (!ctx->cub_tmp) {
+        CK(cub::DeviceRadixSort::SortPairs(nullptr, ctx->cub_bytes, ctx->rk[0], ctx->rk[1], ctx->rk[2], ctx->rk[3],
+                                           (int)cap, 0, end_bit, ctx->st));
+        CK(cudaMalloc(&ctx->cub_tmp, ctx->cub_bytes + 256));
+    }
+    const int p = ctx->par;
+    for (int s = 0; s < 2; s++) {
+        CK(launch_reorder_keys(ctx->g, ctx->sp[p][s], n[s], ctx->rk[0], ctx->rk[2], ctx->st));
+        size_t bytes = ctx->cub_bytes;
+        // stable LSD radix sort by the reference's cell key (library sort,
+        // off the per-lap path)
+        CK(cub::DeviceRadixSort::SortPairs(ctx->cub_tmp, bytes, ctx->rk[0], ctx->rk[1], ctx->rk[2], ctx->rk[3],
+                                           (int)n[s], 0, end_bit, ctx->st));
+        CK(launch_gather(ctx->sp[p][s], ctx->sp[1 - p][s], ctx->rk[3], n[s], ctx->st));
+        CK(cudaMemcpyAsync(ctx->d_cnt + 2 * (1 - p) + s, ctx->d_cnt + 2 * p + s, sizeof(long long),
+                           cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    ctx->par ^= 1;
+    ctx->dirty = true;  // grouped by cell, not by tile
+    ctx->lapreorder = lap;
+    return TG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fused lap
+// ---------------------------------------------------------------------------
+static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk) {
+    cudaStream_t st = ctx->st;
+    const Geom &g = ctx->g;
+    int k = 0;
+    // bc_b1; bc_e1; advance_Bhalfstep; bc_b1  (tristanmainloop.F90:117-122)
+    CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
+    CK(launch_ghost(g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, st)); k++;
+    CK(launch_advance_b(g, ctx->P, ctx->f, st)); k++;
+    CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
+    if (g.dims == 3) { CK(launch_primal(g, ctx->f, ctx->prim, st)); k++; }
+    // reset_currents (:175), then move_particles + deposit_particles fused
+    // (:134, :183): the deposit reads no field and the field updates read
+    // no current, so the current is deposited right after each push
+    if (!ctx->P.fixed)
+        for (int a = 6; a < 9; a++) CK(cudaMemsetAsync(ctx->f[a], 0, (size_t)g.lot * 4, st));
+    TileArgs a = tile_args(ctx, sort_now);
+    CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++;
+    // advance_Bhalfstep; bc_b1; bc_b2 (:139-145); advance_Efield; bc_e2
+    CK(launch_advance_b(g, ctx->P, ctx->f, st)); k++;
+    CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
+    CK(launch_advance_e(g, ctx->P, ctx->f, st)); k++;
+    CK(launch_ghost(g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, st)); k++;
+    if (ctx->P.fixed) {
+        float *cur3[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
+        CK(launch_fixed_to_float(g, ctx->P, ctx->fix, cur3, st)); k++;
+    }
+    // exchange_current; apply_filter1_opt; add_current (:201-242)
+    CK(launch_fold(g, ctx->P, ctx->f + 6, st)); k += g.dims;
+    int r = filter_passes(ctx);
+    if (r) return r;
+    k += ctx->cfg.ntimes;
+    CK(launch_add_current(g, ctx->f, st)); k++;
+    if (sort_now) {
+        int rr = sort_all(ctx, true);
+        if (rr) return rr;
+        k += 4;
+    }
+    *nk = k;
+    return TG_OK;
+}
+
+static int capture_cycle(tg_ctx *ctx, int start_par) {
+    const int se = ctx->cfg.sort_every < 1 ? 1 : ctx->cfg.sort_every;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    int r = TG_OK, nk = 0;
+    for (int l = 0; l < 2 * se && r == TG_OK; l++) r = lap_kernels(ctx, (l % se) == se - 1, &nk);
+    cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
+    if (r) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+    }
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ctx->cycle[start_par], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    ctx->kernels_per_step = nk;
+    // capturing walked the parity through two sorts: back where it started
+    ctx->par = start_par;
+    return TG_OK;
+}
+
+extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
+    if (!ctx || nsteps < 0) return TG_ERR_ARG;
+    int r = ensure_sorted(ctx);
+    if (r) return r;
+    const int se = ctx->cfg.sort_every < 1 ? 1 : ctx->cfg.sort_every;
+    const int cyc = 2 * se;
+    int left = nsteps;
+    // laps are replayed in whole sort cycles from a graph; the phase within a
+    // cycle is tracked by the lap counter
+    while (left > 0) {
+        const int phase = (int)(ctx->lap % cyc);
+        if (phase == 0 && left >= cyc) {
+            const int p = ctx->par;
+            if (!ctx->cycle[p]) {
+                if ((r = capture_cycle(ctx, p))) return r;
+            }
+            CK(cudaGraphLaunch(ctx->cycle[p], ctx->st));
+            // two sorts per cycle: parity unchanged
+            ctx->lap += cyc;
+            left -= cyc;
+        } else {
+            int nk = 0;
+            if ((r = lap_kernels(ctx, (phase % se) == se - 1, &nk))) return r;
+            ctx->kernels_per_step = nk;
+            ctx->lap += 1;
+            left -= 1;
+        }
+    }
+    return TG_OK;
+}
+
+extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
+    if (!ctx || !out) return TG_ERR_ARG;
+    return fail(ctx, TG_ERR_STATE, "tg_diag_fp64: not available in this build");
+}

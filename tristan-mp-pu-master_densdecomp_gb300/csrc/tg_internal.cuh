@@ -1,0 +1,380 @@
+// Internal definitions of the GB300 TRISTAN-MP hot path (sm_103a).
+//
+// Floating point: every file is compiled with -fmad=false and IEEE division
+// and square root, and every expression below is written in the reference
+// Fortran's left-to-right order, so the mover and the field stencils round
+// exactly as the reference does (one rounding per operation, no FMA).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tristan_gpu.h"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// shape-function constants (code/particles.F90:235-248), single precision
+// ---------------------------------------------------------------------------
+#define TG_HALF 0.5f
+#define TG_ONE 1.0f
+#define TG_TWO 2.0f
+#define TG_QUART 0.25f
+#define TG_NINEIGHTH 1.125f
+#define TG_THHALF 1.5f
+#define TG_NEGONE (-1.0f)
+#define TG_TWOTH 0x1.555556p-1f     // 2/3 rounded to single
+#define TG_THIRD 0x1.555556p-2f     // 1/3
+#define TG_SIXTH 0x1.555556p-3f     // 1/6
+#define TG_NEGSIXTH (-0x1.555556p-3f)
+
+// device status bits
+enum : int32_t { ST_BOUNDS = 1, ST_NAN = 2, ST_OVERFLOW = 4, ST_WINDOW = 8 };
+
+// ---------------------------------------------------------------------------
+// Geometry of one domain (derived once at tg_init)
+// ---------------------------------------------------------------------------
+struct Geom {
+    int dims, order;
+    int mx, my, mz;
+    int ng, ngz;
+    long long lot;     // mx*my*mz
+    long long sy, sz;  // strides: sy = mx, sz = mx*my
+    int per[3];
+    // particle position window kept by the periodic wrap
+    float minx, maxx, miny, maxy, minz, maxz;
+    // tiles: origin node of tile (0,0,0) and tile edges, tile counts
+    int tx, ty, tz;
+    int ox, oy, oz;
+    int ntx, nty, ntz;
+    int ntiles;
+    // deposit window (per tile) = tile + [lo, hi] halo per axis
+    int wlo, whi;  // halo below / above the tile, same on every axis
+    int wx, wy, wz;
+    int wcells;
+};
+
+// particle storage: structure of arrays, cell index + in-cell offset
+struct Species {
+    int32_t *cell;  // 0-based linear index of node (aint x, aint y, aint z)
+    float *ox, *oy;  // x - aint(x), y - aint(y)
+    float *oz;       // 3D: z - aint(z); 2D: absolute z (not part of the cell)
+    float *u, *v, *w, *ch;
+    int32_t *ind, *proc, *splitlev;
+};
+
+struct Params {
+    float c, corr, qm[2], qs[2];
+    int external_fields;
+    float ext[6];
+    double x1in, x2in, y1in, y2in, z1in, z2in;
+    long long mxcum, mycum, mzcum;
+    int fixed;
+    float fx_scale;    // 2^fx_shift
+    double fx_inv;     // 2^-fx_shift
+    int quirks;
+};
+
+// ---------------------------------------------------------------------------
+// index helpers (1-based Fortran cell -> 0-based linear)
+// ---------------------------------------------------------------------------
+__host__ __device__ inline long long lin(const Geom &g, int i, int j, int k) {
+    return (long long)(i - 1) + g.sy * (long long)(j - 1) + g.sz * (long long)(k - 1);
+}
+
+__device__ inline void cell_ijk(const Geom &g, int32_t cell, int &i, int &j, int &k) {
+    int c = cell;
+    i = c % g.mx + 1;
+    c /= g.mx;
+    if (g.dims == 3) {
+        j = c % g.my + 1;
+        k = c / g.my + 1;
+    } else {
+        j = c + 1;
+        k = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shape factors. Weights of the NS nonzero slots starting at slot `base`
+// (slot 3 = node aint(x)); identical forms in the movers and deposits
+// (code/particles.F90:738-745, :928-1020, :1175-1277).
+// ---------------------------------------------------------------------------
+template <int ORDER> struct ShapeN;
+template <> struct ShapeN<1> { static constexpr int NS = 2; static constexpr int U = 3; };
+template <> struct ShapeN<2> { static constexpr int NS = 3; static constexpr int U = 5; };
+template <> struct ShapeN<3> { static constexpr int NS = 4; static constexpr int U = 5; };
+
+template <int ORDER>
+__device__ __forceinline__ void shape(float d, float *w, int &base) {
+    if (ORDER == 1) {
+        w[0] = TG_ONE - d;
+        w[1] = d;
+        base = 3;
+    } else if (ORDER == 2) {
+        if (d <= TG_HALF) {
+            float s2 = TG_HALF * (d * d - d + TG_QUART);
+            float s4 = s2 + d;
+            float s3 = TG_ONE - s4 - s2;
+            w[0] = s2; w[1] = s3; w[2] = s4;
+            base = 2;
+        } else {
+            float s3 = TG_NINEIGHTH - TG_THHALF * d + TG_HALF * d * d;
+            float s5 = s3 - TG_ONE + d;
+            float s4 = TG_ONE - s5 - s3;
+            w[0] = s3; w[1] = s4; w[2] = s5;
+            base = 3;
+        }
+    } else {
+        if (d <= TG_HALF) {
+            float s2 = TG_NEGSIXTH * (d - TG_ONE) * (d - TG_ONE) * (d - TG_ONE);
+            float s3 = TG_TWOTH + TG_HALF * (d - TG_TWO) * d * d;
+            float s5 = TG_SIXTH * d * d * d;
+            float s4 = TG_ONE - s5 - s3 - s2;
+            w[0] = s2; w[1] = s3; w[2] = s4; w[3] = s5;
+        } else {
+            float s5 = TG_SIXTH * d * d * d;
+            float s4 = TG_TWOTH + TG_HALF * (TG_NEGONE - d) * (TG_ONE - d) * (TG_ONE - d);
+            float s2 = TG_SIXTH * (TG_ONE - d) * (TG_ONE - d) * (TG_ONE - d);
+            float s3 = TG_ONE - s5 - s4 - s2;
+            w[0] = s2; w[1] = s3; w[2] = s4; w[3] = s5;
+        }
+        base = 2;
+    }
+}
+
+// weight w[s - off] for static s, runtime off in [0, 2] (zero outside)
+template <int NS>
+__device__ __forceinline__ float pick(const float *w, int s, int off) {
+    float r = 0.0f;
+#pragma unroll
+    for (int o = 0; o <= 2; o++) {
+        int idx = s - o;
+        if (idx >= 0 && idx < NS && off == o) r = w[idx];
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Fields seen by the particle kernels
+// ---------------------------------------------------------------------------
+struct FieldPtrs {
+    const float *ex, *ey, *ez, *bx, *by, *bz;          // staggered Yee (2D gather)
+    const float *pex, *pey, *pez, *pbx, *pby, *pbz;    // primal copies (3D gather)
+};
+
+// ---------------------------------------------------------------------------
+// Mover: shape-consistent gather + Boris + position advance, in absolute
+// coordinates (mover_{1,2,3}ord, code/particles_movedeposit.F90:356-1271).
+// The gather loops run over the dual shape's slot range (Q1 for order 2);
+// 2D reads the staggered arrays with mixed weights, 3D the primal copies.
+// ---------------------------------------------------------------------------
+template <int DIM, int ORDER>
+__device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f, const Params &P, float qm,
+                                              float &x, float &y, float &z, float &u, float &v, float &w) {
+    constexpr int NS = ShapeN<ORDER>::NS;
+    const float c = P.c;
+    const float cinv = 1.0f / c;
+    int ip = (int)truncf(x);
+    float dxp = x - (float)ip;
+    int jp = (int)truncf(y);
+    float dyp = y - (float)jp;
+    int kp = (int)truncf(z);
+    int id = (int)truncf(x - TG_HALF);
+    float dxd = x - TG_HALF - (float)id;
+    int jd = (int)truncf(y - TG_HALF);
+    float dyd = y - TG_HALF - (float)jd;
+    int kd = (int)truncf(z - TG_HALF);
+
+    float wxp[NS], wyp[NS], wxd[NS], wyd[NS], wzp[NS], wzd[NS];
+    int bxp, byp, bxd, byd, bzp = 0, bzd = 0;
+    shape<ORDER>(dxp, wxp, bxp);
+    shape<ORDER>(dyp, wyp, byp);
+    shape<ORDER>(dxd, wxd, bxd);
+    shape<ORDER>(dyd, wyd, byd);
+    if (DIM == 3) {
+        float dzp = z - (float)kp;
+        float dzd = (z - TG_HALF) - (float)kd;
+        shape<ORDER>(dzp, wzp, bzp);
+        shape<ORDER>(dzd, wzd, bzd);
+    }
+    // primal weights seen through the dual slot range
+    float axp[NS], ayp[NS], azp[NS];
+#pragma unroll
+    for (int r = 0; r < NS; r++) {
+        if (ORDER == 2) {
+            axp[r] = pick<NS>(wxp, r + 1, bxp - bxd + 1);
+            ayp[r] = pick<NS>(wyp, r + 1, byp - byd + 1);
+            if (DIM == 3) azp[r] = pick<NS>(wzp, r + 1, bzp - bzd + 1);
+        } else {
+            axp[r] = wxp[r];
+            ayp[r] = wyp[r];
+            if (DIM == 3) azp[r] = wzp[r];
+        }
+    }
+    float ex0 = 0.0f, ey0 = 0.0f, ez0 = 0.0f, bx0 = 0.0f, by0 = 0.0f, bz0 = 0.0f;
+    if (DIM == 3) {
+#pragma unroll
+        for (int r3 = 0; r3 < NS; r3++) {
+#pragma unroll
+            for (int r2 = 0; r2 < NS; r2++) {
+                const long long row = (long long)(ip - 3 + bxd - 1) +
+                                      g.sy * (long long)(jp - 3 + byd + r2 - 1) +
+                                      g.sz * (long long)(kp - 3 + bzd + r3 - 1);
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f, sbx = 0.0f, sby = 0.0f, sbz = 0.0f;
+#pragma unroll
+                for (int r1 = 0; r1 < NS; r1++) {
+                    const long long l = row + r1;
+                    sx = sx + __ldg(f.pex + l) * axp[r1];
+                    sy = sy + __ldg(f.pey + l) * axp[r1];
+                    sz = sz + __ldg(f.pez + l) * axp[r1];
+                    sbx = sbx + __ldg(f.pbx + l) * axp[r1];
+                    sby = sby + __ldg(f.pby + l) * axp[r1];
+                    sbz = sbz + __ldg(f.pbz + l) * axp[r1];
+                }
+                ex0 = ex0 + sx * ayp[r2] * azp[r3];
+                ey0 = ey0 + sy * ayp[r2] * azp[r3];
+                ez0 = ez0 + sz * ayp[r2] * azp[r3];
+                bx0 = bx0 + sbx * ayp[r2] * azp[r3];
+                by0 = by0 + sby * ayp[r2] * azp[r3];
+                bz0 = bz0 + sbz * ayp[r2] * azp[r3];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r2 = 0; r2 < NS; r2++) {
+            const long long rowp = g.sy * (long long)(jp - 3 + byd + r2 - 1);
+            const long long rowd = g.sy * (long long)(jd - 3 + byd + r2 - 1);
+#pragma unroll
+            for (int r1 = 0; r1 < NS; r1++) {
+                const long long colp = (long long)(ip - 3 + bxd + r1 - 1);
+                const long long cold = (long long)(id - 3 + bxd + r1 - 1);
+                const long long lpp = colp + rowp, lpd = colp + rowd, ldp = cold + rowp, ldd = cold + rowd;
+                ex0 = ex0 + __ldg(f.ex + ldp) * wxd[r1] * ayp[r2];
+                ey0 = ey0 + __ldg(f.ey + lpd) * axp[r1] * wyd[r2];
+                ez0 = ez0 + __ldg(f.ez + lpp) * axp[r1] * ayp[r2];
+                bx0 = bx0 + __ldg(f.bx + lpd) * axp[r1] * wyd[r2];
+                by0 = by0 + __ldg(f.by + ldp) * wxd[r1] * ayp[r2];
+                bz0 = bz0 + __ldg(f.bz + ldd) * wxd[r1] * wyd[r2];
+            }
+        }
+    }
+    (void)wzd;
+    ex0 = 0.5f * ex0 * qm;
+    ey0 = 0.5f * ey0 * qm;
+    ez0 = 0.5f * ez0 * qm;
+    bx0 = 0.5f * bx0 * qm * cinv;
+    by0 = 0.5f * by0 * qm * cinv;
+    bz0 = 0.5f * bz0 * qm * cinv;
+    if (P.external_fields) {
+        bx0 = bx0 + P.ext[3] * 0.5f * qm * cinv;
+        by0 = by0 + P.ext[4] * 0.5f * qm * cinv;
+        bz0 = bz0 + P.ext[5] * 0.5f * qm * cinv;
+        ex0 = ex0 + P.ext[0] * 0.5f * qm;
+        ey0 = ey0 + P.ext[1] * 0.5f * qm;
+        ez0 = ez0 + P.ext[2] * 0.5f * qm;
+    }
+    // Boris rotation (code/particles_movedeposit.F90:564-583)
+    float u0 = c * u + ex0;
+    float v0 = c * v + ey0;
+    float w0 = c * w + ez0;
+    float gg = c / sqrtf(c * c + u0 * u0 + v0 * v0 + w0 * w0);
+    bx0 = gg * bx0;
+    by0 = gg * by0;
+    bz0 = gg * bz0;
+    float fr = 2.0f / (1.0f + bx0 * bx0 + by0 * by0 + bz0 * bz0);
+    float u1 = (u0 + v0 * bz0 - w0 * by0) * fr;
+    float v1 = (v0 + w0 * bx0 - u0 * bz0) * fr;
+    float w1 = (w0 + u0 * by0 - v0 * bx0) * fr;
+    u0 = u0 + v1 * bz0 - w1 * by0 + ex0;
+    v0 = v0 + w1 * bx0 - u1 * bz0 + ey0;
+    w0 = w0 + u1 * by0 - v1 * bx0 + ez0;
+    u = u0 * cinv;
+    v = v0 * cinv;
+    w = w0 * cinv;
+    gg = c / sqrtf(c * c + u0 * u0 + v0 * v0 + w0 * w0);
+    x = x + u * gg * c;
+    y = y + v * gg * c;
+    z = z + w * gg * c;
+}
+
+// ---------------------------------------------------------------------------
+// Periodic wrap / open-boundary keep test of deposit_particles' boundary
+// loop for one rank (code/particles_movedeposit.F90:1546-1691).
+// Returns false when the particle is discarded.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ bool wrap_particle(const Geom &g, const Params &P, float &x, float &y, float &z) {
+    const float midx = 0.5f * (g.maxx - g.minx), midy = 0.5f * (g.maxy - g.miny), midz = 0.5f * (g.maxz - g.minz);
+    float perx = 0.0f, pery = 0.0f, perz = 0.0f;
+    if (x < g.minx || x > g.maxx) perx = copysignf(midx, x - g.minx) + copysignf(midx, x - g.maxx);
+    if (y < g.miny || y > g.maxy) pery = copysignf(midy, y - g.miny) + copysignf(midy, y - g.maxy);
+    if (z < g.minz || z > g.maxz) perz = copysignf(midz, z - g.minz) + copysignf(midz, z - g.maxz);
+    bool in = true;
+    if (!g.per[0]) {
+        float xg = x + (float)P.mxcum;
+        in = ((double)xg > P.x1in) && ((double)xg < P.x2in);
+    }
+    if (!g.per[1] && in) {
+        float yg = y + (float)P.mycum;
+        in = ((double)yg > P.y1in) && ((double)yg < P.y2in);
+    }
+    if (DIM == 3 && !g.per[2] && in) {
+        float zg = z + (float)P.mzcum;
+        in = ((double)zg > P.z1in) && ((double)zg < P.z2in);
+    }
+    if (!in) {
+        perx = 0.0f; pery = 0.0f; perz = 0.0f;
+    }
+    x = x - perx;
+    y = y - pery;
+    if (DIM == 3 && perz < 0.0f) perz = -((float)g.mz - 1.0f * (float)g.ngz);
+    z = z - perz;
+    return in;
+}
+
+// arguments of the tile kernel (particles sorted by tile)
+struct TileArgs {
+    Geom g;
+    Params P;
+    FieldPtrs f;
+    Species sp[2];
+    const int *tstart[2];  // [ntiles+1] per species
+    int *newcount[2];      // histogram of the particles' new tiles
+    float *cur[3];
+    unsigned long long *fix[3];
+    int *status;
+};
+
+// ---------------------------------------------------------------------------
+// launchers (tg_particles.cu)
+// ---------------------------------------------------------------------------
+cudaError_t launch_tiles(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st);
+cudaError_t launch_push_flat(const Geom &g, const Params &P, const FieldPtrs &f, const Species &sp,
+                             const long long *dcount, long long count, float qm, int *status, cudaStream_t st);
+cudaError_t launch_tile_count(const Geom &g, const Species &sp, const long long *count, long long hint, int *hist,
+                              cudaStream_t st);
+cudaError_t launch_scan(int *hist, int *start, int *cursor, int n, long long *total, cudaStream_t st);
+cudaError_t launch_scatter(const Geom &g, const Species &src, const Species &dst, const long long *count,
+                           long long hint, const int *start, int *cursor, cudaStream_t st);
+cudaError_t launch_gather(const Species &src, const Species &dst, const int *perm, long long count,
+                          cudaStream_t st);
+cudaError_t launch_reorder_keys(const Geom &g, const Species &sp, long long count, int *keys, int *idx,
+                                cudaStream_t st);
+cudaError_t launch_aos_to_soa(const Geom &g, const void *in, const Species &sp, long long count, int *status,
+                              cudaStream_t st);
+cudaError_t launch_soa_to_aos(const Geom &g, const Species &sp, void *out, long long count, cudaStream_t st);
+
+// launchers (tg_fields.cu); fields f[9] = ex ey ez bx by bz curx cury curz
+enum GhostKind { GHOST_BC = 0, GHOST_FILTER = 1 };
+cudaError_t launch_ghost(const Geom &g, float *a, float *b, float *c, GhostKind kind, cudaStream_t st);
+cudaError_t launch_advance_b(const Geom &g, const Params &P, float *const *f, cudaStream_t st);
+cudaError_t launch_advance_e(const Geom &g, const Params &P, float *const *f, cudaStream_t st);
+cudaError_t launch_add_current(const Geom &g, float *const *f, cudaStream_t st);
+cudaError_t launch_fold(const Geom &g, const Params &P, float *const *cur, cudaStream_t st);
+cudaError_t launch_filter_pass(const Geom &g, float *const *in, float *const *out, cudaStream_t st);
+cudaError_t launch_primal(const Geom &g, float *const *f, float *const *pf, cudaStream_t st);
+cudaError_t launch_fixed_to_float(const Geom &g, const Params &P, unsigned long long *const *fx, float *const *cur,
+                                  cudaStream_t st);
+
+}  // namespace tg

@@ -1,0 +1,434 @@
+// Particle kernel templates of the GB300 TRISTAN-MP hot path (sm_103a),
+// included by tg_particles.cu and by the per-(dims, order) tile-kernel
+// translation units tg_tiles_d*o*.cu (split so they compile in parallel).
+//
+//  k_tiles       one CTA per spatial tile: (push) + Esirkepov deposit +
+//                periodic wrap of the tile's particles (both species),
+//                currents accumulated in a shared-memory window (tile plus
+//                stencil halo) and flushed once with global atomics;
+//                counts the particles' new tiles for the next sort.
+//  k_push_flat   the mover alone over a flat particle range (move_particles).
+//  k_tile_count / k_scan_tiles / k_tile_scatter
+//                counting sort of a species into tiles (unstable within a
+//                tile; dead particles dropped).
+//  k_aos_to_soa / k_soa_to_aos
+//                the reference's 40-byte particle records <-> device SoA
+//                (int cell index + in-cell offsets).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "tg_internal.cuh"
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// particle load / store
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ void load_pos(const Geom &g, const Species &s, long long n, float &x, float &y,
+                                         float &z) {
+    int i, j, k;
+    cell_ijk(g, s.cell[n], i, j, k);
+    x = (float)i + s.ox[n];  // exact: ox = x - aint(x)
+    y = (float)j + s.oy[n];
+    z = DIM == 3 ? (float)k + s.oz[n] : s.oz[n];
+}
+
+// cell index of an absolute position; false if outside the array
+template <int DIM>
+__device__ __forceinline__ bool pos_cell(const Geom &g, float x, float y, float z, int &i, int &j, int &k) {
+    if (!(x >= 1.0f && y >= 1.0f && x < (float)(g.mx + 1) && y < (float)(g.my + 1))) return false;
+    i = (int)truncf(x);
+    j = (int)truncf(y);
+    if (DIM == 3) {
+        if (!(z >= 1.0f && z < (float)(g.mz + 1))) return false;
+        k = (int)truncf(z);
+    } else {
+        k = 1;
+    }
+    return true;
+}
+
+// positions whose gather stencil stays inside the array: one cell beyond
+// the wrap window [min, max] on each side
+template <int DIM>
+__device__ __forceinline__ bool gather_safe(const Geom &g, float x, float y, float z) {
+    bool ok = x >= g.minx - 1.0f && x < g.maxx + 1.0f && y >= g.miny - 1.0f && y < g.maxy + 1.0f;
+    if (DIM == 3) ok = ok && z >= g.minz - 1.0f && z < g.maxz + 1.0f;
+    return ok;
+}
+
+__device__ __forceinline__ int tile_of(const Geom &g, int i, int j, int k) {
+    int a = (i - g.ox) / g.tx, b = (j - g.oy) / g.ty, c = g.dims == 3 ? (k - g.oz) / g.tz : 0;
+    a = min(max(a, 0), g.ntx - 1);
+    b = min(max(b, 0), g.nty - 1);
+    c = min(max(c, 0), g.ntz - 1);
+    return a + g.ntx * (b + g.nty * c);
+}
+
+template <int DIM>
+__device__ __forceinline__ void store_pos(const Geom &g, const Species &s, long long n, float x, float y, float z,
+                                          int i, int j, int k) {
+    s.cell[n] = (int32_t)lin(g, i, j, DIM == 3 ? k : 1);
+    s.ox[n] = x - (float)i;
+    s.oy[n] = y - (float)j;
+    s.oz[n] = DIM == 3 ? z - (float)k : z;
+}
+
+// warp-aggregated atomicAdd of 1 to counter[key]; returns this lane's slot
+__device__ __forceinline__ int agg_inc(int *counter, int key) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter + key, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// Deposit sinks
+// ---------------------------------------------------------------------------
+template <bool FIXED>
+struct WindowSink {
+    typedef typename std::conditional<FIXED, unsigned long long, float>::type T;
+    T *s;  // [3][wcells]
+    int wx0, wy0, wz0, wx, wy, wz, wcells;
+    float *gc[3];
+    unsigned long long *gf[3];
+    float scale;
+    const Geom *g;
+    int *status;
+    __device__ __forceinline__ void add(int comp, int i, int j, int k, float v) {
+        const int a = i - wx0, b = j - wy0, c = k - wz0;
+        if ((unsigned)a < (unsigned)wx && (unsigned)b < (unsigned)wy && (unsigned)c < (unsigned)wz) {
+            const int idx = comp * wcells + a + wx * (b + wy * c);
+            if (FIXED) {
+                long long q = __float2ll_rn(v * scale);
+                atomicAdd((unsigned long long *)&s[idx], (unsigned long long)q);
+            } else {
+                atomicAdd((float *)&s[idx], v);
+            }
+        } else {
+            // outside the tile window: straight to global memory
+            if (i < 1 || i > g->mx || j < 1 || j > g->my || k < 1 || k > g->mz) {
+                atomicOr(status, ST_BOUNDS);
+                return;
+            }
+            const long long l = lin(*g, i, j, k);
+            if (FIXED) {
+                long long q = __float2ll_rn(v * scale);
+                atomicAdd(gf[comp] + l, (unsigned long long)q);
+            } else {
+                atomicAdd(gc[comp] + l, v);
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Esirkepov current of one particle moving x1 -> x2
+// (densdecomp_{1,2,3}ord, code/particles.F90:678-1358) in the reference's
+// arithmetic, including the carries that are not reset between rows (x)
+// and planes (y) (Q4). Cells are visited in the reference's order.
+// ---------------------------------------------------------------------------
+template <int DIM, int ORDER, class Sink>
+__device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, float z2, float x1, float y1,
+                                          float z1, float q, Sink &sink, int *status) {
+    constexpr int NS = ShapeN<ORDER>::NS;
+    constexpr int U = ShapeN<ORDER>::U;
+    const int i1 = (int)truncf(x1), i2 = (int)truncf(x2);
+    const int j1 = (int)truncf(y1), j2 = (int)truncf(y2);
+    const int k1 = DIM == 3 ? (int)truncf(z1) : 1;
+    const int k2 = DIM == 3 ? (int)truncf(z2) : 1;
+    const int si = i2 - i1, sj = j2 - j1, sk = k2 - k1;
+    if (si < -1 || si > 1 || sj < -1 || sj > 1 || sk < -1 || sk > 1) {
+        atomicOr(status, ST_BOUNDS);
+        return;
+    }
+    const float dx1 = x1 - truncf(x1), dy1 = y1 - truncf(y1);
+    const float dx2 = x2 - truncf(x2), dy2 = y2 - truncf(y2);
+    float w1x[NS], w2x[NS], w1y[NS], w2y[NS];
+    int b1x, b2x, b1y, b2y;
+    shape<ORDER>(dx1, w1x, b1x);
+    shape<ORDER>(dy1, w1y, b1y);
+    shape<ORDER>(dx2, w2x, b2x);
+    shape<ORDER>(dy2, w2y, b2y);
+    b2x += si;
+    b2y += sj;
+    const int lox = min(b1x, b2x), loy = min(b1y, b2y);
+    const int nx = max(b1x, b2x) + NS - lox, ny = max(b1y, b2y) + NS - loy;
+    float S1x[U], S2x[U], S1y[U], S2y[U];
+#pragma unroll
+    for (int r = 0; r < U; r++) {
+        S1x[r] = pick<NS>(w1x, r, b1x - lox);
+        S2x[r] = pick<NS>(w2x, r, b2x - lox);
+        S1y[r] = pick<NS>(w1y, r, b1y - loy);
+        S2y[r] = pick<NS>(w2y, r, b2y - loy);
+    }
+    const int ibase = i1 - 3 + lox, jbase = j1 - 3 + loy;
+    float cxp = 0.0f;
+    float cyp[U];
+#pragma unroll
+    for (int r = 0; r < U; r++) cyp[r] = 0.0f;
+
+    if (DIM == 2) {
+        const float deltaz = z2 - z1;
+#pragma unroll
+        for (int ry = 0; ry < U; ry++) {
+            if (ry < ny) {
+                const float s1y = S1y[ry], dSy = S2y[ry] - S1y[ry];
+                const float wy = s1y + TG_HALF * dSy;
+#pragma unroll
+                for (int rx = 0; rx < U; rx++) {
+                    if (rx < nx) {
+                        const float s1x = S1x[rx], dSx = S2x[rx] - S1x[rx];
+                        const float cx = q * (dSx * wy) + cxp;
+                        const float cy = q * (dSy * (s1x + TG_HALF * dSx)) + cyp[rx];
+                        const float cz = -(q * deltaz *
+                                           (s1x * s1y + TG_HALF * dSx * s1y + TG_HALF * s1x * dSy +
+                                            TG_THIRD * dSx * dSy));
+                        sink.add(0, ibase + rx, jbase + ry, 1, cx);
+                        sink.add(1, ibase + rx, jbase + ry, 1, cy);
+                        sink.add(2, ibase + rx, jbase + ry, 1, cz);
+                        cxp = cx;
+                        cyp[rx] = cy;
+                    }
+                }
+            }
+        }
+    } else {
+        const float dz1 = z1 - truncf(z1), dz2 = z2 - truncf(z2);
+        float w1z[NS], w2z[NS];
+        int b1z, b2z;
+        shape<ORDER>(dz1, w1z, b1z);
+        shape<ORDER>(dz2, w2z, b2z);
+        b2z += sk;
+        const int loz = min(b1z, b2z);
+        const int nz = max(b1z, b2z) + NS - loz;
+        const int kbase = k1 - 3 + loz;
+        // x-y weights of the z current, one per (x,y) slot
+        float wxy[U][U];
+#pragma unroll
+        for (int rx = 0; rx < U; rx++) {
+#pragma unroll
+            for (int ry = 0; ry < U; ry++) {
+                const float dSx = S2x[rx] - S1x[rx], dSy = S2y[ry] - S1y[ry];
+                wxy[rx][ry] = S1x[rx] * S1y[ry] + TG_HALF * dSx * S1y[ry] + TG_HALF * S1x[rx] * dSy +
+                              TG_THIRD * dSx * dSy;
+            }
+        }
+        float czp[U][U];
+#pragma unroll
+        for (int rx = 0; rx < U; rx++)
+#pragma unroll
+            for (int ry = 0; ry < U; ry++) czp[rx][ry] = 0.0f;
+#pragma unroll
+        for (int rz = 0; rz < U; rz++) {
+            if (rz < nz) {
+                const float s1z = pick<NS>(w1z, rz, b1z - loz);
+                const float dSz = pick<NS>(w2z, rz, b2z - loz) - s1z;
+                float wxz[U];
+#pragma unroll
+                for (int rx = 0; rx < U; rx++) {
+                    const float dSx = S2x[rx] - S1x[rx];
+                    wxz[rx] = S1x[rx] * s1z + TG_HALF * dSx * s1z + TG_HALF * S1x[rx] * dSz + TG_THIRD * dSx * dSz;
+                }
+#pragma unroll
+                for (int ry = 0; ry < U; ry++) {
+                    if (ry < ny) {
+                        const float dSy = S2y[ry] - S1y[ry];
+                        const float wyz = S1y[ry] * s1z + TG_HALF * dSy * s1z + TG_HALF * S1y[ry] * dSz +
+                                          TG_THIRD * dSy * dSz;
+#pragma unroll
+                        for (int rx = 0; rx < U; rx++) {
+                            if (rx < nx) {
+                                const float dSx = S2x[rx] - S1x[rx];
+                                const float cx = q * (dSx * wyz) + cxp;
+                                const float cy = q * (dSy * wxz[rx]) + cyp[rx];
+                                const float cz = q * (dSz * wxy[rx][ry]) + czp[rx][ry];
+                                sink.add(0, ibase + rx, jbase + ry, kbase + rz, cx);
+                                sink.add(1, ibase + rx, jbase + ry, kbase + rz, cy);
+                                sink.add(2, ibase + rx, jbase + ry, kbase + rz, cz);
+                                cxp = cx;
+                                cyp[rx] = cy;
+                                czp[rx][ry] = cz;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The tile kernel
+// ---------------------------------------------------------------------------
+template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
+__global__ void __launch_bounds__(256) k_tiles(TileArgs a) {
+    typedef typename WindowSink<FIXED>::T T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *win = reinterpret_cast<T *>(smem_raw);
+    const Geom &g = a.g;
+    const int tile = blockIdx.x;
+    const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
+    WindowSink<FIXED> sink;
+    sink.s = win;
+    sink.wx0 = g.ox + tix * g.tx - g.wlo;
+    sink.wy0 = g.oy + tiy * g.ty - g.wlo;
+    sink.wz0 = DIM == 3 ? g.oz + tiz * g.tz - g.wlo : 1;
+    sink.wx = g.wx;
+    sink.wy = g.wy;
+    sink.wz = g.wz;
+    sink.wcells = g.wcells;
+    for (int cc = 0; cc < 3; cc++) {
+        sink.gc[cc] = a.cur[cc];
+        sink.gf[cc] = a.fix[cc];
+    }
+    sink.scale = a.P.fx_scale;
+    sink.g = &a.g;
+    sink.status = a.status;
+    if (DEPOSIT) {
+        for (int t = threadIdx.x; t < 3 * g.wcells; t += blockDim.x) win[t] = (T)0;
+        __syncthreads();
+    }
+#pragma unroll 1
+    for (int s = 0; s < 2; s++) {
+        const Species sp = a.sp[s];
+        const int beg = a.tstart[s][tile], end = a.tstart[s][tile + 1];
+        const float qm = a.P.qm[s];
+        const float qs = a.P.qs[s];
+#pragma unroll 1
+        for (int n = beg + threadIdx.x; n < end; n += blockDim.x) {
+            if (sp.cell[n] < 0) continue;  // discarded since the last sort
+            float x, y, z;
+            load_pos<DIM>(g, sp, n, x, y, z);
+            float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+            if (PUSH) {
+                if (!gather_safe<DIM>(g, x, y, z)) {
+                    atomicOr(a.status, ST_BOUNDS);
+                    sp.cell[n] = -1;
+                    continue;
+                }
+                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
+            }
+            bool keep = true;
+            if (DEPOSIT) {
+                // reconstruct the previous position from the new momentum
+                // (deposit_particles, code/particles_movedeposit.F90:1384-1390)
+                const float c = a.P.c;
+                const float invgam = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
+                const float x0 = x - u * invgam * c;
+                const float y0 = y - v * invgam * c;
+                const float z0 = z - w * invgam * c;
+                const float q = sp.ch[n] * qs;
+                esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
+                keep = wrap_particle<DIM>(g, a.P, x, y, z);
+            }
+            int i, j, k;
+            const bool fin = isfinite(x) && isfinite(y) && isfinite(z);
+            if (!fin) atomicOr(a.status, ST_NAN);
+            if (keep && fin && pos_cell<DIM>(g, x, y, z, i, j, k)) {
+                store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
+                if (a.newcount[s]) agg_inc(a.newcount[s], tile_of(g, i, j, k));
+            } else {
+                if (keep) atomicOr(a.status, ST_BOUNDS);
+                sp.cell[n] = -1;  // discarded: dropped by the next sort
+            }
+            if (PUSH) {
+                sp.u[n] = u;
+                sp.v[n] = v;
+                sp.w[n] = w;
+            }
+        }
+    }
+    if (DEPOSIT) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
+            const int a0 = t % g.wx, b0 = (t / g.wx) % g.wy, c0 = t / (g.wx * g.wy);
+            const int i = sink.wx0 + a0, j = sink.wy0 + b0, k = sink.wz0 + c0;
+            const bool inside = i >= 1 && i <= g.mx && j >= 1 && j <= g.my && k >= 1 && k <= g.mz;
+            const long long l = inside ? lin(g, i, j, k) : 0;
+#pragma unroll
+            for (int cc = 0; cc < 3; cc++) {
+                const T val = win[cc * g.wcells + t];
+                if (val != (T)0) {
+                    if (!inside) {
+                        atomicOr(a.status, ST_BOUNDS);
+                        continue;
+                    }
+                    if (FIXED) atomicAdd(a.fix[cc] + l, (unsigned long long)val);
+                    else atomicAdd(a.cur[cc] + l, (float)val);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mover alone over [0, count)
+// ---------------------------------------------------------------------------
+template <int DIM, int ORDER>
+__global__ void __launch_bounds__(256) k_push_flat(Geom g, Params P, FieldPtrs f, Species sp,
+                                                   const long long *dcount, float qm, int *status) {
+    const long long count = *dcount;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < count;
+         n += (long long)gridDim.x * blockDim.x) {
+        if (sp.cell[n] < 0) continue;
+        float x, y, z;
+        load_pos<DIM>(g, sp, n, x, y, z);
+        float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+        if (!gather_safe<DIM>(g, x, y, z)) {
+            atomicOr(status, ST_BOUNDS);
+            sp.cell[n] = -1;
+            continue;
+        }
+        push_particle<DIM, ORDER>(g, f, P, qm, x, y, z, u, v, w);
+        int i, j, k;
+        if (isfinite(x) && isfinite(y) && isfinite(z) && pos_cell<DIM>(g, x, y, z, i, j, k)) {
+            store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
+        } else {
+            atomicOr(status, isfinite(x) && isfinite(y) && isfinite(z) ? ST_BOUNDS : ST_NAN);
+            sp.cell[n] = -1;
+        }
+        sp.u[n] = u;
+        sp.v[n] = v;
+        sp.w[n] = w;
+    }
+}
+
+}  // namespace tg
+
+namespace tg {
+template <int DIM, int ORDER>
+cudaError_t launch_tiles_o(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st,
+                                  size_t smem) {
+    dim3 grid(a.g.ntiles), block(256);
+#define TG_L(F, PU, DE)                                                                              \
+    do {                                                                                             \
+        auto kern = k_tiles<DIM, ORDER, F, PU, DE>;                                                  \
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                             (int)smem);                                             \
+        if (e != cudaSuccess) return e;                                                              \
+        kern<<<grid, block, smem, st>>>(a);                                                          \
+        return cudaGetLastError();                                                                   \
+    } while (0)
+    (void)deposit;  // push-only runs use k_push_flat
+    if (fixed) {
+        if (push) TG_L(true, true, true);
+        TG_L(true, false, true);
+    } else {
+        if (push) TG_L(false, true, true);
+        TG_L(false, false, true);
+    }
+#undef TG_L
+}
+
+
+template <int DIM, int ORDER>
+cudaError_t launch_tiles_o(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st, size_t smem);
+}  // namespace tg

@@ -1,0 +1,6 @@
+// Tile kernels (push + Esirkepov deposit + wrap) for 3D, shape order 1.
+#include "tg_particles.cuh"
+
+namespace tg {
+template cudaError_t launch_tiles_o<3, 1>(const TileArgs &, bool, bool, bool, cudaStream_t, size_t);
+}  // namespace tg

@@ -1,0 +1,284 @@
+"""Host-side mirror of the reference's per-step subroutines over the C-ABI.
+
+``GpuSim`` owns the host arrays the reference keeps in its modules (fields
+``ex..curz`` in Fortran order, the particle array ``p`` with ions at
+``p[0:ions]`` and electrons at ``p[maxhlf:maxhlf+lecs]``) and calls
+``libtristan_gpu.so`` (declared in include/tristan_gpu.h) through ctypes. Its
+method names follow the reference subroutines: ``bc_b1``, ``bc_e1``,
+``advance_Bhalfstep``, ``advance_Efield``, ``move_particles``,
+``reset_currents``, ``deposit_particles``, ``exchange_current``,
+``apply_filter1_opt``, ``add_current``, ``reorder_particles`` and ``step``
+(one lap of the main loop). Errors raise ``TristanGpuError`` with the
+library's message, as the reference prints and stops.
+
+There is no CPU fallback: if the library is not built or no GPU is present
+the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .config import SimConfig
+from .setups import PARTICLE_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libtristan_gpu.so")
+
+TG_OK, TG_ERR_ARG, TG_ERR_CUDA, TG_ERR_OVERFLOW, TG_ERR_BOUNDS, TG_ERR_NAN, TG_ERR_STATE = range(7)
+SYNC_E, SYNC_B, SYNC_CUR, SYNC_PARTICLES, SYNC_ALL = 1, 2, 4, 8, 15
+QUIRK_Q5_LHS = 1
+DEPOSIT_FP32, DEPOSIT_FIXED = 0, 1
+
+FIELD_NAMES = ("ex", "ey", "ez", "bx", "by", "bz", "curx", "cury", "curz")
+
+
+class TristanGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[tg error {code}] {msg}")
+        self.code = code
+
+
+class tg_config(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int32), ("order", ctypes.c_int32),
+        ("mx", ctypes.c_int32), ("my", ctypes.c_int32), ("mz", ctypes.c_int32),
+        ("nghost", ctypes.c_int32), ("nghostz", ctypes.c_int32),
+        ("periodic", ctypes.c_int32 * 3), ("ntimes", ctypes.c_int32), ("quirks", ctypes.c_int32),
+        ("c", ctypes.c_float), ("corr", ctypes.c_float), ("qi", ctypes.c_float), ("qe", ctypes.c_float),
+        ("qmi", ctypes.c_float), ("qme", ctypes.c_float),
+        ("external_fields", ctypes.c_int32), ("ext", ctypes.c_float * 6),
+        ("x1in", ctypes.c_double), ("x2in", ctypes.c_double), ("y1in", ctypes.c_double),
+        ("y2in", ctypes.c_double), ("z1in", ctypes.c_double), ("z2in", ctypes.c_double),
+        ("mxcum", ctypes.c_int64), ("mycum", ctypes.c_int64), ("mzcum", ctypes.c_int64),
+        ("deposit_mode", ctypes.c_int32), ("fx_shift", ctypes.c_int32),
+        ("maxhlf", ctypes.c_int64),
+        ("sort_every", ctypes.c_int32), ("tile", ctypes.c_int32 * 3), ("device", ctypes.c_int32),
+    ]
+
+
+class tg_diag(ctypes.Structure):
+    _fields_ = [
+        ("gauss_residual", ctypes.c_double), ("gauss_abs", ctypes.c_double),
+        ("rho_norm", ctypes.c_double), ("e_field", ctypes.c_double), ("e_mag", ctypes.c_double),
+        ("e_kin_ions", ctypes.c_double), ("e_kin_lecs", ctypes.c_double),
+        ("p_part", ctypes.c_double * 3), ("p_field", ctypes.c_double * 3),
+        ("charge_total", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+ENTRY_POINTS = (
+    "tg_init", "tg_finalize", "tg_last_error", "tg_bind_fields", "tg_bind_particles",
+    "tg_sync_from_host", "tg_sync_to_host", "tg_bc_b1", "tg_bc_e1", "tg_advance_b_half",
+    "tg_advance_e", "tg_move", "tg_reset_currents", "tg_deposit", "tg_fold_currents",
+    "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_diag_fp64", "tg_synchronize",
+    "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step",
+)
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libtristan_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    lib.tg_init.argtypes = [ctypes.POINTER(tg_config), ctypes.POINTER(P)]
+    lib.tg_init.restype = ctypes.c_int
+    lib.tg_finalize.argtypes = [P]
+    lib.tg_finalize.restype = None
+    lib.tg_last_error.argtypes = [P]
+    lib.tg_last_error.restype = ctypes.c_char_p
+    lib.tg_bind_fields.argtypes = [P] + [P] * 9
+    lib.tg_bind_fields.restype = ctypes.c_int
+    lib.tg_bind_particles.argtypes = [P, P, P, P]
+    lib.tg_bind_particles.restype = ctypes.c_int
+    for n in ("tg_sync_from_host", "tg_sync_to_host"):
+        getattr(lib, n).argtypes = [P, ctypes.c_uint]
+        getattr(lib, n).restype = ctypes.c_int
+    for n in ("tg_bc_b1", "tg_bc_e1", "tg_advance_b_half", "tg_advance_e", "tg_move", "tg_reset_currents",
+              "tg_deposit", "tg_fold_currents", "tg_filter", "tg_add_current", "tg_synchronize"):
+        getattr(lib, n).argtypes = [P]
+        getattr(lib, n).restype = ctypes.c_int
+    lib.tg_reorder.argtypes = [P, ctypes.c_int32, ctypes.c_int32]
+    lib.tg_reorder.restype = ctypes.c_int
+    lib.tg_step.argtypes = [P, ctypes.c_int32]
+    lib.tg_step.restype = ctypes.c_int
+    lib.tg_diag_fp64.argtypes = [P, ctypes.POINTER(tg_diag)]
+    lib.tg_diag_fp64.restype = ctypes.c_int
+    lib.tg_get_counts.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    lib.tg_get_counts.restype = ctypes.c_int
+    lib.tg_device_fields.argtypes = [P, ctypes.POINTER(P)]
+    lib.tg_device_fields.restype = ctypes.c_int
+    lib.tg_stream.argtypes = [P]
+    lib.tg_stream.restype = P
+    lib.tg_kernels_per_step.argtypes = [P]
+    lib.tg_kernels_per_step.restype = ctypes.c_int32
+    _lib = lib
+    return lib
+
+
+def make_tg_config(cfg: SimConfig, device: int = 0) -> tg_config:
+    c = tg_config()
+    c.dims, c.order = cfg.dims, cfg.order
+    c.mx, c.my, c.mz = cfg.mx, cfg.my, cfg.mz
+    c.nghost, c.nghostz = cfg.nghost, cfg.nghostz
+    for a in range(3):
+        c.periodic[a] = int(cfg.periodic[a])
+    c.ntimes, c.quirks = cfg.ntimes, cfg.quirks
+    c.c, c.corr = cfg.c, cfg.corr
+    c.qi, c.qe, c.qmi, c.qme = cfg.qi, cfg.qe, cfg.qmi, cfg.qme
+    c.external_fields = int(cfg.external_fields)
+    for a in range(6):
+        c.ext[a] = float(cfg.ext[a])
+    c.x1in, c.x2in, c.y1in, c.y2in, c.z1in, c.z2in = cfg.window_in()
+    c.mxcum = c.mycum = c.mzcum = 0
+    c.deposit_mode = DEPOSIT_FIXED if cfg.fixed else DEPOSIT_FP32
+    c.fx_shift = cfg.fx_shift
+    c.maxhlf = cfg.maxhlf
+    c.sort_every = max(1, int(cfg.sort_every))
+    for a in range(3):
+        c.tile[a] = int(cfg.tile[a])
+    c.device = device
+    return c
+
+
+class GpuSim:
+    """One device domain plus the host arrays it syncs with."""
+
+    def __init__(self, cfg: SimConfig, device: int = 0):
+        self.cfg = cfg
+        self.lib = load_library()
+        self.tcfg = make_tg_config(cfg, device)
+        h = ctypes.c_void_p()
+        rc = self.lib.tg_init(ctypes.byref(self.tcfg), ctypes.byref(h))
+        if rc != TG_OK:
+            raise TristanGpuError(rc, self.lib.tg_last_error(None).decode())
+        self.h = h
+        n = cfg.mx * cfg.my * cfg.mz
+        self.lot = n
+        self.fields = {k: np.zeros(n, np.float32) for k in FIELD_NAMES}
+        self.p = np.zeros(2 * cfg.maxhlf, PARTICLE_DTYPE)
+        self._ions = ctypes.c_int32(0)
+        self._lecs = ctypes.c_int32(0)
+        self._check(self.lib.tg_bind_fields(self.h, *[self.fields[k].ctypes.data for k in FIELD_NAMES]))
+        self._check(self.lib.tg_bind_particles(self.h, self.p.ctypes.data, ctypes.addressof(self._ions),
+                                               ctypes.addressof(self._lecs)))
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tg_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != TG_OK:
+            raise TristanGpuError(rc, self.lib.tg_last_error(self.h).decode())
+
+    # -- host <-> device -----------------------------------------------------
+    def set_particles(self, ions: np.ndarray, lecs: np.ndarray, upload: bool = True) -> None:
+        mh = self.cfg.maxhlf
+        if len(ions) > mh or len(lecs) > mh:
+            raise TristanGpuError(TG_ERR_OVERFLOW, "particle count exceeds maxhlf")
+        self.p[: len(ions)] = ions
+        self.p[mh: mh + len(lecs)] = lecs
+        self._ions.value, self._lecs.value = len(ions), len(lecs)
+        if upload:
+            self.sync_from_host(SYNC_PARTICLES)
+
+    def set_fields(self, **arrays) -> None:
+        for k, v in arrays.items():
+            self.fields[k][:] = np.asarray(v, np.float32).ravel()
+
+    def sync_from_host(self, mask: int = SYNC_ALL) -> None:
+        self._check(self.lib.tg_sync_from_host(self.h, mask))
+
+    def sync_to_host(self, mask: int = SYNC_ALL) -> None:
+        self._check(self.lib.tg_sync_to_host(self.h, mask))
+
+    @property
+    def ions(self) -> np.ndarray:
+        return self.p[: self._ions.value]
+
+    @property
+    def lecs(self) -> np.ndarray:
+        mh = self.cfg.maxhlf
+        return self.p[mh: mh + self._lecs.value]
+
+    def counts(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.tg_get_counts(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    # -- the reference's per-lap subroutines ------------------------------
+    def bc_b1(self):
+        self._check(self.lib.tg_bc_b1(self.h))
+
+    def bc_e1(self):
+        self._check(self.lib.tg_bc_e1(self.h))
+
+    def advance_Bhalfstep(self):
+        self._check(self.lib.tg_advance_b_half(self.h))
+
+    def advance_Efield(self):
+        self._check(self.lib.tg_advance_e(self.h))
+
+    def move_particles(self):
+        self._check(self.lib.tg_move(self.h))
+
+    def reset_currents(self):
+        self._check(self.lib.tg_reset_currents(self.h))
+
+    def deposit_particles(self):
+        self._check(self.lib.tg_deposit(self.h))
+
+    def exchange_current(self):
+        self._check(self.lib.tg_fold_currents(self.h))
+
+    def apply_filter1_opt(self):
+        self._check(self.lib.tg_filter(self.h))
+
+    def add_current(self):
+        self._check(self.lib.tg_add_current(self.h))
+
+    def reorder_particles(self, lap: int, force: bool = False):
+        self._check(self.lib.tg_reorder(self.h, int(lap), 1 if force else 0))
+
+    def step(self, n: int = 1):
+        self._check(self.lib.tg_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(self.lib.tg_synchronize(self.h))
+
+    def kernels_per_step(self) -> int:
+        return int(self.lib.tg_kernels_per_step(self.h))
+
+    def diagnostics(self) -> dict:
+        d = tg_diag()
+        self._check(self.lib.tg_diag_fp64(self.h, ctypes.byref(d)))
+        out = {k: getattr(d, k) for k, _ in tg_diag._fields_}
+        out["p_part"] = list(d.p_part)
+        out["p_field"] = list(d.p_field)
+        return out
+
+    def field(self, name: str) -> np.ndarray:
+        c = self.cfg
+        return self.fields[name].reshape(c.mz, c.my, c.mx)
