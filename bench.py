@@ -1,0 +1,314 @@
+"""Benchmark: particle-steps/s of the TRISTAN-MP hot path on one GB300.
+
+Workload (default): the 2D two-stream/Weibel box of 1024 x 1024 cells,
+3rd-order shapes, 16 particles per cell per species (33.5 M particles),
+4 filter passes, FP64 Gauss-law / energy / momentum diagnostics every lap.
+A "step" is one full lap of the main loop: field advance, push, Esirkepov
+deposit, periodic wrap, current fold, filter, add_current, tile sort and
+the diagnostics. Inputs are seeded synthetic plasmas with the reference
+setup's shapes (tristan_gb300.setups); the particle arrays (~2 GB) are far
+larger than the 129 MB L2, so no flush is needed between laps.
+
+Arms:
+  default           the GB300 C-ABI library; prints one JSON line with the
+                    FP32-atomic form as `value`, the int64 fixed-point form
+                    beside it, the dominant kernel's roofline, the CPU
+                    baseline, the end-to-end figure and the SM clocks.
+  --impl reference  the reference algorithm on the host cores: the OpenMP
+                    build of the CPU restatement (no Fortran compiler exists
+                    on the box, so the reference itself cannot be built).
+
+Multi-GPU: the path does not shard (one domain, no collectives); N ranks
+run N independent replicas and `value` sums them (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__  # noqa: E402
+
+METRIC = "particle-steps/s (push+deposit+fields), batched/fixed-pt vs plain, same GB300"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="twostream2d_1024_o3")
+    ap.add_argument("--no-fixed", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--sort-every", type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws, local):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, ws, impl):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if impl == "gb300" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (every 200 ms)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        time.sleep(0.25)
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload, form):
+    """per-launch DRAM bytes of the tile kernel from the committed ncu summary"""
+    try:
+        with open(os.path.join(ROOT, "profiles", "tile_kernel_traffic.json")) as f:
+            d = json.load(f)
+        return d.get(workload, {}).get(form)
+    except Exception:
+        return None
+
+
+def tile_kernel_bytes(cfg, n_particles, fixed):
+    """algorithmic bytes of one push+deposit launch: per particle read
+    cell+offsets+u+ch (32 B) and write cell+offsets+u (28 B); per cell the
+    gathered E,B (24 B) and the flushed current (12 B, 24 B fixed point)"""
+    return 60.0 * n_particles + (24.0 + (24.0 if fixed else 12.0)) * cfg.ncells
+
+
+def run_form(pkg, cfg, ions, lecs, args, fixed, device, ws, local, clocks=False):
+    from tristan_gb300.gpu import GpuSim
+    cfg.fixed = int(fixed)
+    sim = GpuSim(cfg, device=device)
+    sim.set_particles(ions, lecs)
+    sim.step(max(args.warmup, 3))
+    sim.synchronize()
+    sim.enable_timing(True)
+    barrier(ws, local)
+    sim.synchronize()
+    if clocks:
+        with ClockSampler(device) as cs:
+            ms = sim.step_timed(args.steps)
+        clk = cs.summary()
+    else:
+        ms = sim.step_timed(args.steps)
+        clk = None
+    phases = sim.phase_times()
+    kps = sim.kernels_per_step()
+    hist = sim.diag_history(1)
+    sim.close()
+    return ms, phases, kps, clk, hist
+
+
+def run_e2e(cfg, ions, lecs, args, device):
+    from tristan_gb300.gpu import GpuSim, SYNC_ALL, SYNC_B, SYNC_E, SYNC_PARTICLES
+    cfg.fixed = 0
+    sim = GpuSim(cfg, device=device, pinned=True)
+    sim.set_particles(ions, lecs, upload=False)
+    up = SYNC_E | SYNC_B | SYNC_PARTICLES
+    sim.sync_from_host(SYNC_ALL)
+    sim.step(1)
+    sim.sync_to_host(SYNC_ALL)
+    h2d, d2h = sim.host_bytes(up), sim.host_bytes(SYNC_ALL)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sim.sync_from_host(up)
+        sim.step(1)
+        sim.sync_to_host(SYNC_ALL)
+    dt = time.perf_counter() - t0
+    sim.close()
+    return dt, h2d, d2h
+
+
+def cpu_baseline(cfg, ions, lecs, steps):
+    import oracle
+    oracle.build()
+    cfg.fixed = 0
+    sim = oracle.OracleSim(cfg, openmp=True)
+    sim.set_particles(ions, lecs)
+    sim.step(1)
+    t0 = time.perf_counter()
+    sim.step(steps)
+    dt = time.perf_counter() - t0
+    return dt, sim.lib.to_num_threads()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args)
+    pkg = __graft_entry__.load_package()
+    from tristan_gb300 import setups
+    cfg = setups.make_config(args.workload, diag_every=1, sort_every=args.sort_every)
+    ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    n_p = len(ions) + len(lecs)
+    grid = [cfg.nx, cfg.ny] + ([cfg.nz] if cfg.dims == 3 else [])
+    config = {"workload": args.workload, "grid": grid, "order": cfg.order, "particles": n_p,
+              "ppc_per_species": int(cfg.ppc0 // 2), "ntimes": cfg.ntimes, "deposit": "fp32-atomic",
+              "diagnostics": "fp64 gauss/energy/momentum every lap", "sort_every": cfg.sort_every,
+              "l2": "inputs larger than L2 (particle arrays %.1f GB), no flush" % (n_p * 44 / 1e9)}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import oracle
+        oracle.build()
+        cfg.fixed = 0
+        sim = oracle.OracleSim(cfg, openmp=True)
+        sim.set_particles(ions, lecs)
+        sim.step(max(args.warmup, 0))
+        t0 = time.perf_counter()
+        sim.step(args.steps)
+        dt = time.perf_counter() - t0
+        cores = sim.lib.to_num_threads()
+        value = n_p * args.steps / dt
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{args.steps} full laps of the workload, OpenMP CPU restatement "
+                                           "(the reference Fortran cannot be built: no Fortran compiler)"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    device = local
+    ms, phases, kps, clk, hist = run_form(pkg, cfg, ions, lecs, args, False, device, ws, local, clocks=True)
+    ms = allreduce_max(ms, ws, args.impl)
+    value = ws * n_p * args.steps / (ms / 1e3)
+    fixed = None
+    if not args.no_fixed:
+        ms_f, ph_f, _, _, _ = run_form(pkg, cfg, ions, lecs, args, True, device, ws, local)
+        ms_f = allreduce_max(ms_f, ws, args.impl)
+        fixed = {"value": ws * n_p * args.steps / (ms_f / 1e3), "ms_per_step": ms_f / args.steps,
+                 "particle_kernel_ms": ph_f["particles"], "deposit": "int64 fixed point (bit-reproducible)"}
+    dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, args, device)
+    e2e = {"value": ws * n_p * args.e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h,
+           "mode": "every lap: host state -> device (E, B, particles), tg_step, device -> host (all)"}
+    peak, peak_kind = measured_peak_hbm()
+    t_kernel = phases["particles"] / 1e3
+    alg = tile_kernel_bytes(cfg, n_p, False)
+    achieved = alg / t_kernel / 1e9 if t_kernel > 0 else None
+    roofline = {"kernel": "k_tiles (fused push + Esirkepov deposit + wrap)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                "traffic": committed_traffic(args.workload, "fp32"),
+                "algorithmic_bytes_per_launch": alg, "launch_ms": phases["particles"]}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        dt_cpu, cores = cpu_baseline(cfg, ions, lecs, args.cpu_steps)
+        cpu = {"value": n_p * args.cpu_steps / dt_cpu, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_steps} full laps of the workload (after 1 warm-up lap) on the OpenMP "
+                         "CPU restatement; the Fortran reference cannot be built on the box"}
+    if rank != 0:
+        return
+    d = hist[-1] if len(hist) else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config, "fixed_point": fixed, "phase_ms_per_lap": phases,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": kps * args.steps,
+            "gauss_residual_last_lap": (float(np.sqrt(d[0] / d[1])) if d is not None and d[1] > 0 else None)}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,6 +81,7 @@ typedef struct {
     int32_t sort_every;  /* re-sort particles into tiles every k laps (>= 1) */
     int32_t tile[3];     /* tile edge in cells (0 = automatic) */
     int32_t device;      /* CUDA device ordinal */
+    int32_t diag_every;  /* 1: FP64 diagnostics inside every tg_step lap */
 } tg_config;
 
 typedef struct tg_ctx tg_ctx;
@@ -157,9 +158,28 @@ int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force);
    (code/tristanmainloop.F90:115-303 without output, injection and domain
    moves), fused and replayed from a captured CUDA graph. */
 int tg_step(tg_ctx *ctx, int32_t nsteps);
+/* tg_step bracketed by CUDA events on the context's stream; *ms receives
+   the device time of the nsteps laps. Synchronises. */
+int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms);
 /* FP64 Gauss-law residual, energies and momenta of the device state.
    Synchronises. */
 int tg_diag_fp64(tg_ctx *ctx, tg_diag *out);
+
+/* Per-lap FP64 diagnostics recorded by tg_step when diag_every = 1: the
+   last n records, oldest first, 16 doubles each in the order
+   |div E - F(rho)|^2, |F(rho)|^2, total charge, E energy, B energy, ion and
+   electron kinetic energy, particle momentum x/y/z, field momentum x/y/z,
+   2 unused. Returns the number of records written. Synchronises. */
+int tg_diag_history(tg_ctx *ctx, double *out, int32_t n);
+
+/* Phase timing with CUDA events recorded on the context's stream inside
+   tg_step (and inside its captured graph). on != 0 enables it (graphs are
+   re-captured). tg_phase_times returns, per lap of the last tg_step launch,
+   the mean milliseconds of: [0] field update before the push, [1] the fused
+   push + deposit kernel, [2] field update after the push, [3] current fold,
+   filter and add_current, [4] tile sort, [5] FP64 diagnostics. */
+int tg_enable_timing(tg_ctx *ctx, int32_t on);
+int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases);
 
 /* Wait for all work on the context's stream; returns any device status. */
 int tg_synchronize(tg_ctx *ctx);

@@ -36,7 +36,7 @@ def test_config_struct_layout():
     c = gpu.tg_config
     assert c.x1in.offset % 8 == 0
     assert c.maxhlf.offset % 8 == 0
-    assert ctypes.sizeof(c) == 216
+    assert ctypes.sizeof(c) == 216  # includes diag_every (fits the tail padding)
 
 
 def test_no_cpu_fallback_without_library(tmp_path):

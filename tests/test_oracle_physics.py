@@ -1,0 +1,114 @@
+"""Physics known-answer tests that pin the oracle where the reference ships
+no golden vectors: B-spline partition of unity, per-particle discrete charge
+continuity of the Esirkepov current, Gauss's law under the binomial filter
+over a Weibel run, and the Yee vacuum dispersion relation with Corr."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from tristan_gb300 import setups
+from tristan_gb300.config import SimConfig
+
+ORDERS = [(2, 1), (2, 2), (2, 3), (3, 1), (3, 2), (3, 3)]
+
+
+def one_particle_sim(dims, order, ntimes=0):
+    cfg = SimConfig(dims=dims, order=order, nx=12, ny=12, nz=12 if dims == 3 else 1, ntimes=ntimes, maxhlf=4)
+    return cfg, oracle.OracleSim(cfg)
+
+
+def rho_of(sim, x, y, z, q=1.0):
+    p = np.zeros(1, oracle.PARTICLE_DTYPE)
+    p["x"], p["y"], p["z"], p["ch"] = x, y, z, 1.0
+    sim.set_particles(p, p[:0])
+    sim.st.qi = q
+    return sim.charge_density()
+
+
+@pytest.mark.parametrize("dims,order", ORDERS)
+def test_partition_of_unity(dims, order):
+    cfg, sim = one_particle_sim(dims, order)
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        x, y, z = rng.uniform(6, 10, 3).astype(np.float32)
+        rho = rho_of(sim, x, y, z if dims == 3 else 3.5)
+        assert abs(rho.sum() - 1.0) < 1e-6
+
+
+@pytest.mark.parametrize("dims,order", ORDERS)
+def test_esirkepov_discrete_continuity(dims, order):
+    """div(cur) of one particle's deposit equals the change of its
+    B-spline charge, node by node (cur = -J per unit time)."""
+    cfg, sim = one_particle_sim(dims, order)
+    rng = np.random.default_rng(1)
+    q = 1.0
+    mx, my, mz = cfg.mx, cfg.my, cfg.mz
+    for _ in range(12):
+        x1, y1 = rng.uniform(6, 10, 2)
+        z1 = rng.uniform(6, 10) if dims == 3 else 3.5
+        d = rng.uniform(-0.44, 0.44, 3)
+        x2, y2, z2 = x1 + d[0], y1 + d[1], z1 + d[2]
+        x1, y1, z1, x2, y2, z2 = (np.float32(v) for v in (x1, y1, z1, x2, y2, z2))
+        for k in ("curx", "cury", "curz"):
+            sim.fields[k][:] = 0
+        sim.lib.to_densdecomp(sim.ptr, x2, y2, z2, x1, y1, z1, q)
+        cx = sim.fields["curx"].reshape(mz, my, mx).astype(np.float64)
+        cy = sim.fields["cury"].reshape(mz, my, mx).astype(np.float64)
+        cz = sim.fields["curz"].reshape(mz, my, mx).astype(np.float64)
+        div = (cx - np.roll(cx, 1, axis=2)) + (cy - np.roll(cy, 1, axis=1))
+        if dims == 3:
+            div += cz - np.roll(cz, 1, axis=0)
+        r2 = rho_of(sim, x2, y2, z2, q).reshape(mz, my, mx)
+        r1 = rho_of(sim, x1, y1, z1, q).reshape(mz, my, mx)
+        np.testing.assert_allclose(div, r2 - r1, atol=2e-6)
+
+
+@pytest.mark.parametrize("dims,order", [(2, 1), (2, 3), (3, 2)])
+def test_gauss_law_with_filter(dims, order):
+    if dims == 2:
+        cfg = SimConfig(dims=2, order=order, nx=32, ny=32, c_omp=5.0, ppc0=8.0, gamma0=3.0, ntimes=4)
+    else:
+        cfg = SimConfig(dims=3, order=order, nx=12, ny=12, nz=12, c_omp=4.0, ppc0=4.0, gamma0=3.0, ntimes=2)
+    ions, lecs = setups.load_beams(cfg, seed=3)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    sim = oracle.OracleSim(cfg)
+    sim.set_particles(ions, lecs)
+    d0 = sim.diagnostics()
+    assert d0["gauss_abs"] < 1e-12  # neutral start
+    sim.step(10)
+    d = sim.diagnostics()
+    assert d["rho_norm"] > 0
+    assert d["gauss_residual"] < 1e-4, d
+
+
+def test_yee_vacuum_dispersion():
+    """A plane wave along x in an empty periodic box oscillates at the Yee
+    scheme's numerical frequency: sin(w/2) = Corr*c*sin(k/2) (dt = dx = 1)."""
+    nx = 64
+    cfg = SimConfig(dims=2, order=1, nx=nx, ny=8, ntimes=0, maxhlf=4, c=0.45, corr=1.025)
+    sim = oracle.OracleSim(cfg)
+    mode = 2
+    kk = 2 * math.pi * mode / nx
+    ng = cfg.nghost
+    i = np.arange(1, cfg.mx + 1)
+    xe = (i - (ng // 2 + 1)).astype(np.float64)
+    ey = np.cos(kk * xe).astype(np.float32)
+    sim.field("ey")[:] = np.broadcast_to(ey, (cfg.mz, cfg.my, cfg.mx))
+    probe = []
+    for _ in range(400):
+        sim.step()
+        probe.append(float(sim.field("ey")[0, 5, ng // 2 + 1]))
+    probe = np.array(probe)
+    # frequency from the zero crossings of the standing wave
+    s = np.sign(probe)
+    crossings = np.nonzero(s[1:] != s[:-1])[0]
+    t = []
+    for c0 in crossings:
+        a, b = probe[c0], probe[c0 + 1]
+        t.append(c0 + a / (a - b))
+    period = 2 * np.mean(np.diff(t))
+    w_meas = 2 * math.pi / period
+    w_theory = 2 * math.asin(cfg.corr * cfg.c * math.sin(kk / 2))
+    assert abs(w_meas - w_theory) / w_theory < 2e-3

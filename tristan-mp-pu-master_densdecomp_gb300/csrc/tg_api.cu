@@ -18,6 +18,8 @@ using namespace tg;
 
 static thread_local char g_init_error[512];
 
+#define TG_NPHASES 6  // fields before the push, particles, fields after, current, sort, diagnostics
+
 struct tg_ctx {
     tg_config cfg;
     Geom g;
@@ -37,6 +39,7 @@ struct tg_ctx {
     int *tstart[2] = {}, *hist[2] = {}, *cursor[2] = {};
     int *d_status = nullptr;
     bool dirty = true;      // particles not grouped by tile
+    bool may_have_dead = false;  // entries marked discarded since the last sort
     // host bindings
     float *hf[9] = {};
     void *hp = nullptr;
@@ -46,9 +49,21 @@ struct tg_ctx {
     int *rk[4] = {};        // reorder keys in/out, values in/out
     void *cub_tmp = nullptr;
     size_t cub_bytes = 0;
+    // FP64 diagnostics
+    unsigned long long *rhofx = nullptr;
+    double *rho[2] = {};
+    double *dacc = nullptr, *dhist = nullptr;
+    unsigned long long *dcounter = nullptr;
+    int hist_cap = 1024;
     // graphs: one cycle of 2*sort_every laps per starting parity
     cudaGraphExec_t cycle[2] = {nullptr, nullptr};
     int kernels_per_step = 0;
+    // phase timing: events per lap of a cycle, [lap][phase][begin/end]
+    bool timing = false;
+    std::vector<cudaEvent_t> ev;
+    int ev_laps = 0;
+    int last_laps = 0;       // laps covered by the last launch (graph or direct)
+    bool ev_used[64][TG_NPHASES] = {};
     long long lap = 0;
     long long lapreorder = 0;
     char err[512] = {0};
@@ -245,6 +260,21 @@ extern "C" int tg_init(const tg_config *cfg, tg_ctx **out) {
         if (!r) r = dalloc(ctx, &ctx->cursor[s], (size_t)g.ntiles);
     }
     if (!r) r = dalloc(ctx, &ctx->d_status, 1);
+    {
+        const size_t nint = (size_t)(g.mx - g.ng) * (g.my - g.ng) * (g.dims == 3 ? g.mz - g.ngz : 1);
+        if (!r) r = dalloc(ctx, &ctx->rhofx, nint);
+        if (!r) r = dalloc(ctx, &ctx->rho[0], nint);
+        if (!r) r = dalloc(ctx, &ctx->rho[1], nint);
+        if (!r) r = dalloc(ctx, &ctx->dacc, 16);
+        if (!r) r = dalloc(ctx, &ctx->dhist, (size_t)ctx->hist_cap * 16);
+        if (!r) r = dalloc(ctx, &ctx->dcounter, 1);
+        if (!r) {
+            e = cudaMemsetAsync(ctx->rhofx, 0, nint * 8, ctx->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dacc, 0, 16 * 8, ctx->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dhist, 0, (size_t)ctx->hist_cap * 16 * 8, ctx->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dcounter, 0, 8, ctx->st);
+        }
+    }
     if (r) {
         snprintf(g_init_error, sizeof g_init_error, "%s", ctx->err);
         tg_finalize(ctx);
@@ -278,6 +308,7 @@ extern "C" void tg_finalize(tg_ctx *ctx) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     for (int p = 0; p < 2; p++)
         if (ctx->cycle[p]) cudaGraphExecDestroy(ctx->cycle[p]);
+    for (auto &e : ctx->ev) cudaEventDestroy(e);
     for (void *q : ctx->allocs) cudaFree(q);
     if (ctx->stage) cudaFree(ctx->stage);
     for (int a = 0; a < 4; a++)
@@ -325,6 +356,7 @@ static int sort_all(tg_ctx *ctx, bool counted) {
     if ((r = sort_species(ctx, 1, counted))) return r;
     ctx->par ^= 1;
     ctx->dirty = false;
+    ctx->may_have_dead = false;
     return TG_OK;
 }
 
@@ -410,10 +442,13 @@ extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
     return TG_OK;
 }
 
-// current counts of the buffer in use (drops discarded particles first)
+// current counts of the buffer in use (drops discarded particles first; the
+// order of a buffer without discarded entries is left as it is)
 static int exact_counts(tg_ctx *ctx, long long n[2]) {
-    int r = ensure_sorted(ctx);
-    if (r) return r;
+    if (ctx->may_have_dead) {
+        int r = sort_all(ctx, false);
+        if (r) return r;
+    }
     CK(cudaMemcpyAsync(n, ctx->d_cnt + 2 * ctx->par, 2 * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->hcount[0] = n[0];
@@ -501,6 +536,7 @@ extern "C" int tg_move(tg_ctx *ctx) {
         CK(launch_push_flat(ctx->g, ctx->P, fp, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,
                             ctx->hcount[s], ctx->P.qm[s], ctx->d_status, ctx->st));
     ctx->dirty = true;
+    ctx->may_have_dead = true;
     return TG_OK;
 }
 
@@ -523,6 +559,7 @@ extern "C" int tg_deposit(tg_ctx *ctx) {
         CK(launch_fixed_to_float(ctx->g, ctx->P, ctx->fix, cur3, ctx->st));
     }
     ctx->dirty = true;  // wrapped particles left their tiles
+    ctx->may_have_dead = true;
     return TG_OK;
 }
 
@@ -596,12 +633,77 @@ extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
 }
 
 // ---------------------------------------------------------------------------
+// FP64 diagnostics
+// ---------------------------------------------------------------------------
+static int run_diag(tg_ctx *ctx) {
+    DiagLaunch d;
+    memset(&d, 0, sizeof d);
+    d.g = ctx->g;
+    d.P = ctx->P;
+    for (int s = 0; s < 2; s++) {
+        d.sp[s] = ctx->sp[ctx->par][s];
+        d.tstart[s] = ctx->tstart[s];
+        d.mass[s] = fabsf(ctx->P.qs[s] / ctx->P.qm[s]);
+    }
+    for (int a = 0; a < 6; a++) d.f[a] = ctx->f[a];
+    d.rhofx = ctx->rhofx;
+    d.rho[0] = ctx->rho[0];
+    d.rho[1] = ctx->rho[1];
+    d.acc = ctx->dacc;
+    d.hist = ctx->dhist;
+    d.hist_cap = ctx->hist_cap;
+    d.counter = ctx->dcounter;
+    d.ntimes = ctx->cfg.ntimes;
+    d.status = ctx->d_status;
+    CK(launch_diag(d, ctx->st));
+    return TG_OK;
+}
+
+static void record_to_diag(const double *h, tg_diag *out) {
+    memset(out, 0, sizeof *out);
+    out->gauss_abs = sqrt(h[0]);
+    out->rho_norm = sqrt(h[1]);
+    out->gauss_residual = h[1] > 0.0 ? sqrt(h[0] / h[1]) : sqrt(h[0]);
+    out->charge_total = h[2];
+    out->e_field = h[3];
+    out->e_mag = h[4];
+    out->e_kin_ions = h[5];
+    out->e_kin_lecs = h[6];
+    for (int a = 0; a < 3; a++) {
+        out->p_part[a] = h[7 + a];
+        out->p_field[a] = h[10 + a];
+    }
+}
+
+extern "C" int tg_diag_history(tg_ctx *ctx, double *out, int32_t n) {
+    if (!ctx || !out || n < 0) return TG_ERR_ARG;
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, ctx->dcounter, 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    long long have = (long long)cnt < ctx->hist_cap ? (long long)cnt : ctx->hist_cap;
+    if (n > have) n = (int32_t)have;
+    for (int32_t r = 0; r < n; r++) {
+        const unsigned long long idx = (cnt - (unsigned long long)n + (unsigned long long)r) % (unsigned long long)ctx->hist_cap;
+        CK(cudaMemcpyAsync(out + (size_t)r * 16, ctx->dhist + idx * 16, 16 * 8, cudaMemcpyDeviceToHost, ctx->st));
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    return n;
+}
+
+// ---------------------------------------------------------------------------
 // fused lap
 // ---------------------------------------------------------------------------
-static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk) {
+static cudaError_t mark(tg_ctx *ctx, int li, int phase, int end) {
+    if (!ctx->timing || li >= ctx->ev_laps) return cudaSuccess;
+    if (!end) ctx->ev_used[li][phase] = true;
+    return cudaEventRecord(ctx->ev[((size_t)li * TG_NPHASES + phase) * 2 + end], ctx->st);
+}
+
+static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
     cudaStream_t st = ctx->st;
     const Geom &g = ctx->g;
     int k = 0;
+    CK(mark(ctx, li, 0, 0));
     // bc_b1; bc_e1; advance_Bhalfstep; bc_b1  (tristanmainloop.F90:117-122)
     CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
     CK(launch_ghost(g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, st)); k++;
@@ -613,13 +715,19 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk) {
     // no current, so the current is deposited right after each push
     if (!ctx->P.fixed)
         for (int a = 6; a < 9; a++) CK(cudaMemsetAsync(ctx->f[a], 0, (size_t)g.lot * 4, st));
+    CK(mark(ctx, li, 0, 1));
+    CK(mark(ctx, li, 1, 0));
     TileArgs a = tile_args(ctx, sort_now);
     CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++;
+    CK(mark(ctx, li, 1, 1));
+    CK(mark(ctx, li, 2, 0));
     // advance_Bhalfstep; bc_b1; bc_b2 (:139-145); advance_Efield; bc_e2
     CK(launch_advance_b(g, ctx->P, ctx->f, st)); k++;
     CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
     CK(launch_advance_e(g, ctx->P, ctx->f, st)); k++;
     CK(launch_ghost(g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, st)); k++;
+    CK(mark(ctx, li, 2, 1));
+    CK(mark(ctx, li, 3, 0));
     if (ctx->P.fixed) {
         float *cur3[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
         CK(launch_fixed_to_float(g, ctx->P, ctx->fix, cur3, st)); k++;
@@ -630,10 +738,20 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk) {
     if (r) return r;
     k += ctx->cfg.ntimes;
     CK(launch_add_current(g, ctx->f, st)); k++;
+    CK(mark(ctx, li, 3, 1));
     if (sort_now) {
+        CK(mark(ctx, li, 4, 0));
         int rr = sort_all(ctx, true);
         if (rr) return rr;
         k += 4;
+        CK(mark(ctx, li, 4, 1));
+    }
+    if (ctx->cfg.diag_every > 0) {
+        CK(mark(ctx, li, 5, 0));
+        int rr = run_diag(ctx);
+        if (rr) return rr;
+        k += 4 + ctx->cfg.ntimes;
+        CK(mark(ctx, li, 5, 1));
     }
     *nk = k;
     return TG_OK;
@@ -644,7 +762,7 @@ static int capture_cycle(tg_ctx *ctx, int start_par) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     int r = TG_OK, nk = 0;
-    for (int l = 0; l < 2 * se && r == TG_OK; l++) r = lap_kernels(ctx, (l % se) == se - 1, &nk);
+    for (int l = 0; l < 2 * se && r == TG_OK; l++) r = lap_kernels(ctx, (l % se) == se - 1, &nk, l);
     cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
     if (r) {
         if (graph) cudaGraphDestroy(graph);
@@ -664,6 +782,7 @@ extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
     if (!ctx || nsteps < 0) return TG_ERR_ARG;
     int r = ensure_sorted(ctx);
     if (r) return r;
+    if (nsteps > 0) ctx->may_have_dead = true;
     const int se = ctx->cfg.sort_every < 1 ? 1 : ctx->cfg.sort_every;
     const int cyc = 2 * se;
     int left = nsteps;
@@ -680,9 +799,11 @@ extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
             // two sorts per cycle: parity unchanged
             ctx->lap += cyc;
             left -= cyc;
+            ctx->last_laps = cyc;
         } else {
             int nk = 0;
-            if ((r = lap_kernels(ctx, (phase % se) == se - 1, &nk))) return r;
+            if ((r = lap_kernels(ctx, (phase % se) == se - 1, &nk, 0))) return r;
+            ctx->last_laps = 1;
             ctx->kernels_per_step = nk;
             ctx->lap += 1;
             left -= 1;
@@ -691,7 +812,69 @@ extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
     return TG_OK;
 }
 
+extern "C" int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms) {
+    if (!ctx || !ms) return TG_ERR_ARG;
+    int r = ensure_sorted(ctx);
+    if (r) return r;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, ctx->st));
+    r = tg_step(ctx, nsteps);
+    CK(cudaEventRecord(b, ctx->st));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (r) return r;
+    return check_status(ctx);
+}
+
+extern "C" int tg_enable_timing(tg_ctx *ctx, int32_t on) {
+    if (!ctx) return TG_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int p = 0; p < 2; p++)
+        if (ctx->cycle[p]) {
+            cudaGraphExecDestroy(ctx->cycle[p]);
+            ctx->cycle[p] = nullptr;
+        }
+    if (on && ctx->ev.empty()) {
+        const int se = ctx->cfg.sort_every < 1 ? 1 : ctx->cfg.sort_every;
+        ctx->ev_laps = 2 * se < 64 ? 2 * se : 64;
+        ctx->ev.resize((size_t)ctx->ev_laps * TG_NPHASES * 2);
+        for (auto &e : ctx->ev) CK(cudaEventCreate(&e));
+    }
+    ctx->timing = on != 0;
+    memset(ctx->ev_used, 0, sizeof ctx->ev_used);
+    return TG_OK;
+}
+
+extern "C" int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases) {
+    if (!ctx || !ms) return TG_ERR_ARG;
+    if (!ctx->timing) return fail(ctx, TG_ERR_STATE, "tg_phase_times: timing not enabled");
+    CK(cudaStreamSynchronize(ctx->st));
+    const int laps = ctx->last_laps < ctx->ev_laps ? ctx->last_laps : ctx->ev_laps;
+    for (int ph = 0; ph < nphases && ph < TG_NPHASES; ph++) {
+        float sum = 0.0f;
+        for (int li = 0; li < laps; li++) {
+            if (!ctx->ev_used[li][ph]) continue;
+            float t = 0.0f;
+            const size_t b = ((size_t)li * TG_NPHASES + ph) * 2;
+            CK(cudaEventElapsedTime(&t, ctx->ev[b], ctx->ev[b + 1]));
+            sum += t;
+        }
+        ms[ph] = laps > 0 ? sum / (float)laps : 0.0f;
+    }
+    return TG_OK;
+}
+
 extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
     if (!ctx || !out) return TG_ERR_ARG;
-    return fail(ctx, TG_ERR_STATE, "tg_diag_fp64: not available in this build");
+    int r = ensure_sorted(ctx);
+    if (r) return r;
+    if ((r = run_diag(ctx))) return r;
+    double h[16];
+    if (tg_diag_history(ctx, h, 1) != 1) return fail(ctx, TG_ERR_STATE, "tg_diag_fp64: no record");
+    record_to_diag(h, out);
+    return check_status(ctx);
 }

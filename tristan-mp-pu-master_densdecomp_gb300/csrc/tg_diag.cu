@@ -1,0 +1,300 @@
+// FP64 diagnostics of the GB300 TRISTAN-MP hot path (sm_103a).
+//
+// Gauss's law with the binomial filter: the deposit is charge conserving
+// and the filter (a periodic convolution) commutes with the divergence, so
+// with a neutral start div E = F^ntimes(rho) at every lap, rho the charge
+// deposited with the same B-spline. Per lap:
+//  k_diag_particles  one CTA per tile: rho in an int64 fixed-point shared
+//                    window (products in FP32, one rounding to 2^-fx_shift,
+//                    so the sum is order independent), kinetic energy
+//                    (gamma-1 = u^2/(gamma+1) in FP32) and momentum summed
+//                    in FP64;
+//  k_rho_to_double   fixed point -> FP64 on the periodic interior;
+//  k_filter64        one FP64 binomial pass on the periodic interior;
+//  k_diag_fields     FP64 reductions: |div E - F(rho)|^2, |F(rho)|^2, total
+//                    charge, field energies and E x B momentum;
+//  k_diag_finish     writes the lap's record into the history ring.
+// GB300 has little FP64 throughput, so FP64 is used only where the sums
+// need it (accumulators and the per-cell field reductions).
+#include <cuda_runtime.h>
+
+#include "tg_particles.cuh"
+
+namespace tg {
+
+enum { D_RES2 = 0, D_RHO2, D_CHARGE, D_EE, D_EB, D_EKI, D_EKE, D_PX, D_PY, D_PZ, D_FX, D_FY, D_FZ, D_N = 16 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-reduce `vals[NV]` and add the block total to acc[first..]
+template <int NV>
+__device__ __forceinline__ void block_accumulate(double *vals, double *acc, int first) {
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) vals[q] = warp_sum(vals[q]);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) red[wid][q] = vals[q];
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double v = lane < nw ? red[lane][q] : 0.0;
+            v = warp_sum(v);
+            if (lane == 0 && v != 0.0) atomicAdd(acc + first + q, v);
+        }
+    }
+}
+
+struct DiagArgs {
+    Geom g;
+    Params P;
+    Species sp[2];
+    const int *tstart[2];
+    unsigned long long *rhofx;  // interior, periodic
+    double *acc;                // [D_N]
+    float mass[2];              // |q/qm| per species
+    int *status;
+};
+
+__device__ __forceinline__ int wrap_i(int i, int lo, int n) {
+    int r = (i - lo) % n;
+    if (r < 0) r += n;
+    return r;
+}
+
+template <int DIM, int ORDER>
+__global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
+    constexpr int NS = ShapeN<ORDER>::NS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned long long *win = reinterpret_cast<unsigned long long *>(smem_raw);
+    const Geom &g = a.g;
+    const int tile = blockIdx.x;
+    const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
+    const int wx0 = g.ox + tix * g.tx - g.wlo, wy0 = g.oy + tiy * g.ty - g.wlo;
+    const int wz0 = DIM == 3 ? g.oz + tiz * g.tz - g.wlo : 1;
+    const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
+    const int lox = g.ng / 2 + 1, loz = g.ngz / 2 + 1;
+    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) win[t] = 0ull;
+    __syncthreads();
+    double part[7] = {0, 0, 0, 0, 0, 0, 0};  // eki, eke, px, py, pz, pad
+    for (int s = 0; s < 2; s++) {
+        const Species sp = a.sp[s];
+        const int beg = a.tstart[s][tile], end = a.tstart[s][tile + 1];
+        const float qs = a.P.qs[s], m = a.mass[s];
+        for (int n = beg + threadIdx.x; n < end; n += blockDim.x) {
+            const int cell = sp.cell[n];
+            if (cell < 0) continue;
+            int i, j, k;
+            cell_ijk(g, cell, i, j, k);
+            const float ox = sp.ox[n], oy = sp.oy[n];
+            const float oz = DIM == 3 ? sp.oz[n] : 0.0f;
+            const float q = sp.ch[n] * qs;
+            float wx[NS], wy[NS], wz[NS];
+            int bx, by, bz = 3;
+            shape<ORDER>(ox, wx, bx);
+            shape<ORDER>(oy, wy, by);
+            if (DIM == 3) shape<ORDER>(oz, wz, bz);
+            else wz[0] = 1.0f;
+            constexpr int NZ = DIM == 3 ? NS : 1;
+#pragma unroll
+            for (int c = 0; c < NZ; c++) {
+#pragma unroll
+                for (int b = 0; b < NS; b++) {
+                    const float qyz = q * wy[b] * wz[c];
+#pragma unroll
+                    for (int aa = 0; aa < NS; aa++) {
+                        const float v = qyz * wx[aa];
+                        const long long fxv = __float2ll_rn(v * a.P.fx_scale);
+                        const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
+                        const int ra = ii - wx0, rb = jj - wy0, rc = kk - wz0;
+                        if ((unsigned)ra < (unsigned)g.wx && (unsigned)rb < (unsigned)g.wy &&
+                            (unsigned)rc < (unsigned)g.wz) {
+                            atomicAdd(&win[ra + g.wx * (rb + g.wy * rc)], (unsigned long long)fxv);
+                        } else {
+                            const long long l = wrap_i(ii, lox, nx) +
+                                                (long long)nx * (wrap_i(jj, lox, ny) +
+                                                                 (long long)ny * (DIM == 3 ? wrap_i(kk, loz, nz) : 0));
+                            atomicAdd(a.rhofx + l, (unsigned long long)fxv);
+                        }
+                    }
+                }
+            }
+            const float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+            const float u2 = u * u + v * v + w * w;
+            const float gm1 = u2 / (sqrtf(1.0f + u2) + 1.0f);
+            const float mc = m * sp.ch[n];
+            part[s] += (double)(gm1 * mc);
+            part[2] += (double)(mc * u);
+            part[3] += (double)(mc * v);
+            part[4] += (double)(mc * w);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
+        const unsigned long long val = win[t];
+        if (val == 0ull) continue;
+        const int ra = t % g.wx, rb = (t / g.wx) % g.wy, rc = t / (g.wx * g.wy);
+        const long long l = wrap_i(wx0 + ra, lox, nx) +
+                            (long long)nx * (wrap_i(wy0 + rb, lox, ny) +
+                                             (long long)ny * (DIM == 3 ? wrap_i(wz0 + rc, loz, nz) : 0));
+        atomicAdd(a.rhofx + l, val);
+    }
+    block_accumulate<5>(part, a.acc, D_EKI);
+}
+
+__global__ void k_rho_to_double(long long n, double inv, unsigned long long *fx, double *rho) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        rho[t] = __ll2double_rn((long long)fx[t]) * inv;
+        fx[t] = 0ull;
+    }
+}
+
+// one binomial pass on the periodic interior (nx, ny, nz)
+template <int DIM>
+__global__ void k_filter64(int nx, int ny, int nz, const double *__restrict__ in, double *out) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % nx);
+        const long long r = t / nx;
+        const int j = (int)(r % ny), k = (int)(r / ny);
+        const int im = i == 0 ? nx - 1 : i - 1, ip = i == nx - 1 ? 0 : i + 1;
+        const int jm = j == 0 ? ny - 1 : j - 1, jp = j == ny - 1 ? 0 : j + 1;
+        double acc = 0.0;
+        if (DIM == 2) {
+            const double *row = in + (long long)j * nx, *rm = in + (long long)jm * nx, *rp = in + (long long)jp * nx;
+            acc = 4.0 * row[i] + 2.0 * (row[im] + row[ip] + rm[i] + rp[i]) + (rm[im] + rm[ip] + rp[im] + rp[ip]);
+            out[t] = acc * 0.0625;
+        } else {
+            const int km = k == 0 ? nz - 1 : k - 1, kp = k == nz - 1 ? 0 : k + 1;
+            const int ks[3] = {km, k, kp};
+            const double wk[3] = {1.0, 2.0, 1.0};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const long long pl = (long long)ks[c] * ny;
+                const double *row = in + (pl + j) * nx, *rm = in + (pl + jm) * nx, *rp = in + (pl + jp) * nx;
+                acc += wk[c] * (4.0 * row[i] + 2.0 * (row[im] + row[ip] + rm[i] + rp[i]) +
+                                (rm[im] + rm[ip] + rp[im] + rp[ip]));
+            }
+            out[t] = acc * 0.015625;
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__restrict__ ex, const float *__restrict__ ey,
+                                                     const float *__restrict__ ez, const float *__restrict__ bx,
+                                                     const float *__restrict__ by, const float *__restrict__ bz,
+                                                     const double *__restrict__ rho, double *acc) {
+    const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
+    const int lo = g.ng / 2 + 1, loz = DIM == 3 ? g.ngz / 2 + 1 : 1;
+    const long long n = (long long)nx * ny * nz;
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // res2 rho2 charge eE eB fx fy fz
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(t % nx);
+        const long long r = t / nx;
+        const int b = (int)(r % ny), c = (int)(r / ny);
+        const int i = lo + a, j = lo + b, k = loz + c;
+        const long long l = lin(g, i, j, k);
+        const int im = a == 0 ? lo + nx - 1 : i - 1, jm = b == 0 ? lo + ny - 1 : j - 1;
+        double div = (double)ex[l] - (double)ex[lin(g, im, j, k)] + (double)ey[l] - (double)ey[lin(g, i, jm, k)];
+        if (DIM == 3) {
+            const int km = c == 0 ? loz + nz - 1 : k - 1;
+            div += (double)ez[l] - (double)ez[lin(g, i, j, km)];
+        }
+        const double rh = rho[t];
+        const double res = div - rh;
+        v[0] += res * res;
+        v[1] += rh * rh;
+        v[2] += rh;
+        const double e0 = ex[l], e1 = ey[l], e2 = ez[l], b0 = bx[l], b1 = by[l], b2 = bz[l];
+        v[3] += 0.5 * (e0 * e0 + e1 * e1 + e2 * e2);
+        v[4] += 0.5 * (b0 * b0 + b1 * b1 + b2 * b2);
+        v[5] += e1 * b2 - e2 * b1;
+        v[6] += e2 * b0 - e0 * b2;
+        v[7] += e0 * b1 - e1 * b0;
+    }
+    double first[5] = {v[0], v[1], v[2], v[3], v[4]};
+    block_accumulate<5>(first, acc, D_RES2);
+    __syncthreads();
+    double second[3] = {v[5], v[6], v[7]};
+    block_accumulate<3>(second, acc, D_FX);
+}
+
+// copy the lap's accumulators into the history ring and clear them
+__global__ void k_diag_finish(double *acc, double *hist, int cap, unsigned long long *counter) {
+    const unsigned long long slot = *counter % (unsigned long long)cap;
+    if (threadIdx.x < D_N) {
+        hist[slot * D_N + threadIdx.x] = acc[threadIdx.x];
+        acc[threadIdx.x] = 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter += 1ull;
+}
+
+static int dgrid(long long n) {
+    long long b = (n + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 152 * 8) b = 152 * 8;
+    return (int)b;
+}
+
+cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
+    const Geom &g = d.g;
+    DiagArgs a;
+    a.g = g;
+    a.P = d.P;
+    for (int s = 0; s < 2; s++) {
+        a.sp[s] = d.sp[s];
+        a.tstart[s] = d.tstart[s];
+        a.mass[s] = d.mass[s];
+    }
+    a.rhofx = d.rhofx;
+    a.acc = d.acc;
+    a.status = d.status;
+    const size_t smem = (size_t)g.wcells * 8;
+    cudaError_t e;
+#define TG_DL(D, O)                                                                                     \
+    do {                                                                                                \
+        e = cudaFuncSetAttribute(k_diag_particles<D, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                 (int)smem);                                                            \
+        if (e != cudaSuccess) return e;                                                                 \
+        k_diag_particles<D, O><<<g.ntiles, 256, smem, st>>>(a);                                         \
+    } while (0)
+    if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
+    else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
+    else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
+    else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);
+    else if (g.dims == 3 && g.order == 2) TG_DL(3, 2);
+    else TG_DL(3, 3);
+#undef TG_DL
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = g.dims == 3 ? g.mz - g.ngz : 1;
+    const long long n = (long long)nx * ny * nz;
+    k_rho_to_double<<<dgrid(n), 256, 0, st>>>(n, d.P.fx_inv, d.rhofx, d.rho[0]);
+    double *cur = d.rho[0], *nxt = d.rho[1];
+    for (int p = 0; p < d.ntimes; p++) {
+        if (g.dims == 3) k_filter64<3><<<dgrid(n), 256, 0, st>>>(nx, ny, nz, cur, nxt);
+        else k_filter64<2><<<dgrid(n), 256, 0, st>>>(nx, ny, nz, cur, nxt);
+        double *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    if (g.dims == 3)
+        k_diag_fields<3><<<dgrid(n), 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+    else
+        k_diag_fields<2><<<dgrid(n), 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+    k_diag_finish<<<1, 32, 0, st>>>(d.acc, d.hist, d.hist_cap, d.counter);
+    return cudaGetLastError();
+}
+
+}  // namespace tg

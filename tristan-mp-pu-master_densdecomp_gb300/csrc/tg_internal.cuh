@@ -365,6 +365,25 @@ cudaError_t launch_aos_to_soa(const Geom &g, const void *in, const Species &sp, 
                               cudaStream_t st);
 cudaError_t launch_soa_to_aos(const Geom &g, const Species &sp, void *out, long long count, cudaStream_t st);
 
+// FP64 diagnostics (tg_diag.cu)
+struct DiagLaunch {
+    Geom g;
+    Params P;
+    Species sp[2];
+    const int *tstart[2];
+    float mass[2];
+    const float *f[6];
+    unsigned long long *rhofx;  // periodic interior, fixed point
+    double *rho[2];             // periodic interior, FP64 ping-pong
+    double *acc;                // 16 accumulators
+    double *hist;               // history ring [hist_cap][16]
+    int hist_cap;
+    unsigned long long *counter;
+    int ntimes;
+    int *status;
+};
+cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
+
 // launchers (tg_fields.cu); fields f[9] = ex ey ez bx by bz curx cury curz
 enum GhostKind { GHOST_BC = 0, GHOST_FILTER = 1 };
 cudaError_t launch_ghost(const Geom &g, float *a, float *b, float *c, GhostKind kind, cudaStream_t st);

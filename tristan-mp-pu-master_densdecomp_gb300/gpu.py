@@ -56,6 +56,7 @@ class tg_config(ctypes.Structure):
         ("deposit_mode", ctypes.c_int32), ("fx_shift", ctypes.c_int32),
         ("maxhlf", ctypes.c_int64),
         ("sort_every", ctypes.c_int32), ("tile", ctypes.c_int32 * 3), ("device", ctypes.c_int32),
+        ("diag_every", ctypes.c_int32),
     ]
 
 
@@ -76,8 +77,10 @@ ENTRY_POINTS = (
     "tg_sync_from_host", "tg_sync_to_host", "tg_bc_b1", "tg_bc_e1", "tg_advance_b_half",
     "tg_advance_e", "tg_move", "tg_reset_currents", "tg_deposit", "tg_fold_currents",
     "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_diag_fp64", "tg_synchronize",
-    "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step",
+    "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step", "tg_diag_history",
+    "tg_enable_timing", "tg_phase_times", "tg_step_timed",
 )
+PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
@@ -120,6 +123,14 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_stream.restype = P
     lib.tg_kernels_per_step.argtypes = [P]
     lib.tg_kernels_per_step.restype = ctypes.c_int32
+    lib.tg_diag_history.argtypes = [P, ctypes.c_void_p, ctypes.c_int32]
+    lib.tg_diag_history.restype = ctypes.c_int
+    lib.tg_step_timed.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]
+    lib.tg_step_timed.restype = ctypes.c_int
+    lib.tg_enable_timing.argtypes = [P, ctypes.c_int32]
+    lib.tg_enable_timing.restype = ctypes.c_int
+    lib.tg_phase_times.argtypes = [P, ctypes.c_void_p, ctypes.c_int32]
+    lib.tg_phase_times.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -146,13 +157,37 @@ def make_tg_config(cfg: SimConfig, device: int = 0) -> tg_config:
     for a in range(3):
         c.tile[a] = int(cfg.tile[a])
     c.device = device
+    c.diag_every = int(cfg.diag_every)
     return c
 
 
-class GpuSim:
-    """One device domain plus the host arrays it syncs with."""
+_cudart = None
 
-    def __init__(self, cfg: SimConfig, device: int = 0):
+
+def _cudart_lib():
+    global _cudart
+    if _cudart is None:
+        load_library()  # pulls libcudart in with the C-ABI library
+        for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+            try:
+                _cudart = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        if _cudart is None:
+            raise RuntimeError("libcudart not found")
+        _cudart.cudaHostRegister.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint]
+        _cudart.cudaHostRegister.restype = ctypes.c_int
+        _cudart.cudaHostUnregister.argtypes = [ctypes.c_void_p]
+        _cudart.cudaHostUnregister.restype = ctypes.c_int
+    return _cudart
+
+
+class GpuSim:
+    """One device domain plus the host arrays it syncs with. ``pinned``
+    page-locks the host arrays (cudaHostRegister) for full-speed copies."""
+
+    def __init__(self, cfg: SimConfig, device: int = 0, pinned: bool = False):
         self.cfg = cfg
         self.lib = load_library()
         self.tcfg = make_tg_config(cfg, device)
@@ -167,6 +202,13 @@ class GpuSim:
         self.p = np.zeros(2 * cfg.maxhlf, PARTICLE_DTYPE)
         self._ions = ctypes.c_int32(0)
         self._lecs = ctypes.c_int32(0)
+        self._pinned = []
+        if pinned:
+            rt = _cudart_lib()
+            for arr in [self.p] + [self.fields[k] for k in FIELD_NAMES]:
+                if rt.cudaHostRegister(arr.ctypes.data, arr.nbytes, 0) != 0:
+                    raise TristanGpuError(TG_ERR_CUDA, "cudaHostRegister failed")
+                self._pinned.append(arr)
         self._check(self.lib.tg_bind_fields(self.h, *[self.fields[k].ctypes.data for k in FIELD_NAMES]))
         self._check(self.lib.tg_bind_particles(self.h, self.p.ctypes.data, ctypes.addressof(self._ions),
                                                ctypes.addressof(self._lecs)))
@@ -176,6 +218,23 @@ class GpuSim:
         if getattr(self, "h", None):
             self.lib.tg_finalize(self.h)
             self.h = None
+            for arr in getattr(self, "_pinned", []):
+                _cudart_lib().cudaHostUnregister(arr.ctypes.data)
+            self._pinned = []
+
+    def host_bytes(self, mask: int) -> int:
+        """bytes one sync of `mask` moves (particles at the current counts)"""
+        n = 0
+        per = self.lot * 4
+        if mask & SYNC_E:
+            n += 3 * per
+        if mask & SYNC_B:
+            n += 3 * per
+        if mask & SYNC_CUR:
+            n += 3 * per
+        if mask & SYNC_PARTICLES:
+            n += (self._ions.value + self._lecs.value) * PARTICLE_DTYPE.itemsize
+        return n
 
     def __del__(self):
         try:
@@ -265,6 +324,12 @@ class GpuSim:
     def step(self, n: int = 1):
         self._check(self.lib.tg_step(self.h, int(n)))
 
+    def step_timed(self, n: int) -> float:
+        """n laps bracketed by CUDA events on the library's stream; ms"""
+        ms = ctypes.c_float()
+        self._check(self.lib.tg_step_timed(self.h, int(n), ctypes.byref(ms)))
+        return float(ms.value)
+
     def synchronize(self):
         self._check(self.lib.tg_synchronize(self.h))
 
@@ -278,6 +343,24 @@ class GpuSim:
         out["p_part"] = list(d.p_part)
         out["p_field"] = list(d.p_field)
         return out
+
+    DIAG_KEYS = ("res2", "rho2", "charge_total", "e_field", "e_mag", "e_kin_ions", "e_kin_lecs",
+                 "px", "py", "pz", "fx", "fy", "fz")
+
+    def diag_history(self, n: int) -> np.ndarray:
+        out = np.zeros((n, 16), np.float64)
+        got = self.lib.tg_diag_history(self.h, out.ctypes.data, int(n))
+        if got < 0:
+            self._check(got)
+        return out[:got]
+
+    def enable_timing(self, on: bool = True):
+        self._check(self.lib.tg_enable_timing(self.h, 1 if on else 0))
+
+    def phase_times(self) -> dict:
+        ms = np.zeros(len(PHASES), np.float32)
+        self._check(self.lib.tg_phase_times(self.h, ms.ctypes.data, len(PHASES)))
+        return {k: float(v) for k, v in zip(PHASES, ms)}
 
     def field(self, name: str) -> np.ndarray:
         c = self.cfg
