@@ -860,10 +860,14 @@ extern "C" int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases) {
             if (!ctx->ev_used[li][ph]) continue;
             float t = 0.0f;
             const size_t b = ((size_t)li * TG_NPHASES + ph) * 2;
-            CK(cudaEventElapsedTime(&t, ctx->ev[b], ctx->ev[b + 1]));
+            if (cudaEventElapsedTime(&t, ctx->ev[b], ctx->ev[b + 1]) != cudaSuccess) {
+                (void)cudaGetLastError();
+                sum = -1.0f;  // event pair not timed
+                break;
+            }
             sum += t;
         }
-        ms[ph] = laps > 0 ? sum / (float)laps : 0.0f;
+        ms[ph] = (laps > 0 && sum >= 0.0f) ? sum / (float)laps : -1.0f;
     }
     return TG_OK;
 }
