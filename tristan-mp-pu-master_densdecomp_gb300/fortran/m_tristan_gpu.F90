@@ -1,0 +1,244 @@
+!
+! m_tristan_gpu -- ISO_C_BINDING shim between the TRISTAN-MP main loop and
+! the GB300 C-ABI (include/tristan_gpu.h).
+!
+! The reference main loop (code/tristanmainloop.F90:107-344) calls
+! argument-less module subroutines. This module gives the same names and
+! forwards to libtristan_gpu.so; the module-global arrays of m_fields and
+! m_particles are registered once with tg_bind_fields / tg_bind_particles
+! and synchronised only around host-side work (Diagnostics, output, restart,
+! host user hooks). Compile with the reference's -DtwoD/-Dddk flags and link
+! -ltristan_gpu. Not compiled in this repository (no Fortran compiler).
+!
+#ifdef twoD
+module m_tristan_gpu
+  use m_fields
+  use m_particles
+#else
+module m_tristan_gpu_3d
+  use m_fields_3d
+  use m_particles_3d
+#endif
+  use iso_c_binding
+  implicit none
+  private
+
+  type, bind(C) :: tg_config
+     integer(c_int32_t) :: dims, order, mx, my, mz, nghost, nghostz
+     integer(c_int32_t) :: periodic(3), ntimes, quirks
+     real(c_float) :: c, corr, qi, qe, qmi, qme
+     integer(c_int32_t) :: external_fields
+     real(c_float) :: ext(6)
+     real(c_double) :: x1in, x2in, y1in, y2in, z1in, z2in
+     integer(c_int64_t) :: mxcum, mycum, mzcum
+     integer(c_int32_t) :: deposit_mode, fx_shift
+     integer(c_int64_t) :: maxhlf
+     integer(c_int32_t) :: sort_every, tile(3), device, diag_every
+  end type tg_config
+
+  interface
+     integer(c_int) function tg_init(cfg, ctx) bind(C, name="tg_init")
+       import :: tg_config, c_int, c_ptr
+       type(tg_config), intent(in) :: cfg
+       type(c_ptr), intent(out) :: ctx
+     end function
+     subroutine tg_finalize(ctx) bind(C, name="tg_finalize")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end subroutine
+     type(c_ptr) function tg_last_error(ctx) bind(C, name="tg_last_error")
+       import :: c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_bind_fields(ctx, ex, ey, ez, bx, by, bz, cx, cy, cz) bind(C, name="tg_bind_fields")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, ex, ey, ez, bx, by, bz, cx, cy, cz
+     end function
+     integer(c_int) function tg_bind_particles(ctx, p, ions, lecs) bind(C, name="tg_bind_particles")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, p, ions, lecs
+     end function
+     integer(c_int) function tg_sync_from_host(ctx, mask) bind(C, name="tg_sync_from_host")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: mask
+     end function
+     integer(c_int) function tg_sync_to_host(ctx, mask) bind(C, name="tg_sync_to_host")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: mask
+     end function
+     integer(c_int) function tg_bc_b1(ctx) bind(C, name="tg_bc_b1")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_bc_e1(ctx) bind(C, name="tg_bc_e1")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_advance_b_half(ctx) bind(C, name="tg_advance_b_half")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_advance_e(ctx) bind(C, name="tg_advance_e")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_move(ctx) bind(C, name="tg_move")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_reset_currents(ctx) bind(C, name="tg_reset_currents")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_deposit(ctx) bind(C, name="tg_deposit")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_fold_currents(ctx) bind(C, name="tg_fold_currents")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_filter(ctx) bind(C, name="tg_filter")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_add_current(ctx) bind(C, name="tg_add_current")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_reorder(ctx, lap, force) bind(C, name="tg_reorder")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: lap, force
+     end function
+     integer(c_int) function tg_step(ctx, nsteps) bind(C, name="tg_step")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: nsteps
+     end function
+  end interface
+
+  type(c_ptr), save :: ctx = c_null_ptr
+  integer(c_int), parameter :: SYNC_E = 1, SYNC_B = 2, SYNC_CUR = 4, SYNC_PARTICLES = 8, SYNC_ALL = 15
+
+  public :: tg_start, tg_stop, tg_download, tg_upload, &
+            gpu_bc_b1, gpu_bc_e1, gpu_advance_Bhalfstep, gpu_advance_Efield, gpu_move_particles, &
+            gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
+            gpu_add_current, gpu_reorder_particles, gpu_step
+
+contains
+
+  subroutine check(rc, what)
+    integer(c_int), intent(in) :: rc
+    character(len=*), intent(in) :: what
+    character(kind=c_char), pointer :: msg(:)
+    integer :: n
+    if (rc == 0) return
+    call c_f_pointer(tg_last_error(ctx), msg, [512])
+    n = 0
+    do while (n < 512)
+       if (msg(n + 1) == c_null_char) exit
+       n = n + 1
+    enddo
+    print *, rank, ": ", what, " failed: ", msg(1:n)
+    stop
+  end subroutine check
+
+  ! after read_input_* and allocate_*: the device mirror of one rank's domain
+  subroutine tg_start(deposit_mode, sort_every)
+    integer, intent(in) :: deposit_mode, sort_every
+    type(tg_config) :: cfg
+    cfg%dims = merge(2, 3, mz == 1)
+#ifdef dd1
+    cfg%order = 1
+#endif
+#ifdef dd2
+    cfg%order = 2
+#endif
+#ifdef dd3
+    cfg%order = 3
+#endif
+    cfg%mx = mx; cfg%my = my; cfg%mz = mz
+    cfg%nghost = nghost; cfg%nghostz = nghostz
+    cfg%periodic = [periodicx, periodicy, periodicz]
+    cfg%ntimes = ntimes; cfg%quirks = 0
+    cfg%c = c; cfg%corr = corr
+    cfg%qi = qi; cfg%qe = qe; cfg%qmi = qmi; cfg%qme = qme
+    cfg%external_fields = merge(1, 0, external_fields)
+    cfg%ext = 0.
+    cfg%x1in = x1in; cfg%x2in = x2in; cfg%y1in = y1in; cfg%y2in = y2in; cfg%z1in = z1in; cfg%z2in = z2in
+    cfg%mxcum = mxcum; cfg%mycum = mycum; cfg%mzcum = mzcum
+    cfg%deposit_mode = deposit_mode
+    cfg%fx_shift = 32 - ceiling(log(max(abs(qi), abs(qe))) / log(2.))
+    cfg%maxhlf = maxhlf
+    cfg%sort_every = sort_every
+    cfg%tile = 0; cfg%device = 0; cfg%diag_every = 0
+    call check(tg_init(cfg, ctx), "tg_init")
+    call check(tg_bind_fields(ctx, c_loc(ex), c_loc(ey), c_loc(ez), c_loc(bx), c_loc(by), c_loc(bz), &
+               c_loc(curx), c_loc(cury), c_loc(curz)), "tg_bind_fields")
+    call check(tg_bind_particles(ctx, c_loc(p), c_loc(ions), c_loc(lecs)), "tg_bind_particles")
+    call check(tg_sync_from_host(ctx, SYNC_ALL), "tg_sync_from_host")
+  end subroutine tg_start
+
+  subroutine tg_stop()
+    call tg_finalize(ctx)
+    ctx = c_null_ptr
+  end subroutine tg_stop
+
+  ! before Diagnostics / output / restart / host-side user hooks
+  subroutine tg_download()
+    call check(tg_sync_to_host(ctx, SYNC_ALL), "tg_sync_to_host")
+  end subroutine tg_download
+
+  ! after host-side injection or field_bc_user edits
+  subroutine tg_upload()
+    call check(tg_sync_from_host(ctx, SYNC_ALL), "tg_sync_from_host")
+  end subroutine tg_upload
+
+  subroutine gpu_bc_b1()
+    call check(tg_bc_b1(ctx), "bc_b1")
+  end subroutine
+  subroutine gpu_bc_e1()
+    call check(tg_bc_e1(ctx), "bc_e1")
+  end subroutine
+  subroutine gpu_advance_Bhalfstep()
+    call check(tg_advance_b_half(ctx), "advance_Bhalfstep")
+  end subroutine
+  subroutine gpu_advance_Efield()
+    call check(tg_advance_e(ctx), "advance_Efield")
+  end subroutine
+  subroutine gpu_move_particles()
+    call check(tg_move(ctx), "move_particles")
+  end subroutine
+  subroutine gpu_reset_currents()
+    call check(tg_reset_currents(ctx), "reset_currents")
+  end subroutine
+  subroutine gpu_deposit_particles()
+    call check(tg_deposit(ctx), "deposit_particles")
+  end subroutine
+  subroutine gpu_exchange_current()
+    call check(tg_fold_currents(ctx), "exchange_current")
+  end subroutine
+  subroutine gpu_apply_filter1_opt()
+    call check(tg_filter(ctx), "apply_filter1_opt")
+  end subroutine
+  subroutine gpu_add_current()
+    call check(tg_add_current(ctx), "add_current")
+  end subroutine
+  subroutine gpu_reorder_particles()
+    call check(tg_reorder(ctx, int(lap, c_int32_t), 0_c_int32_t), "reorder_particles")
+  end subroutine
+
+  ! the whole periodic lap fused on the device (replaces lines 115-303)
+  subroutine gpu_step(nsteps)
+    integer, intent(in) :: nsteps
+    call check(tg_step(ctx, int(nsteps, c_int32_t)), "tg_step")
+  end subroutine
+
+#ifdef twoD
+end module m_tristan_gpu
+#else
+end module m_tristan_gpu_3d
+#endif
