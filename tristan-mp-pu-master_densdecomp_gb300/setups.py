@@ -42,6 +42,10 @@ WORKLOADS = {
     # 2D two-stream/Weibel: 1024^2, order 3, 16 ppc/species, beams +-0.5c
     "twostream2d_1024_o3": dict(dims=2, order=3, nx=1024, ny=1024, c=0.45, c_omp=10.0,
                                 ppc0=32.0, gamma0=0.5, delgam=0.005, ntimes=4),
+    # the same plasma on a 512^2 box (8.4 M particles, 370 MB of particle
+    # data: still above L2) for kernel profiling
+    "twostream2d_512_o3": dict(dims=2, order=3, nx=512, ny=512, c=0.45, c_omp=10.0,
+                               ppc0=32.0, gamma0=0.5, delgam=0.005, ntimes=4),
     # 3D Weibel: 256^3, order 2, 4 ppc/species, gamma0 = 5
     "weibel3d_256_o2": dict(dims=3, order=2, nx=256, ny=256, nz=256, c=0.45, c_omp=8.0,
                             ppc0=8.0, gamma0=5.0, delgam=0.01, ntimes=4),
