@@ -181,6 +181,22 @@ int tg_diag_history(tg_ctx *ctx, double *out, int32_t n);
 int tg_enable_timing(tg_ctx *ctx, int32_t on);
 int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases);
 
+/* Binomial current filter (the ntimes passes of apply_filter1_opt) on three
+   caller-owned device arrays of the Fortran (mx,my,mz) layout, allocating
+   nothing. No counterpart in the reference: it exists for callers that
+   cannot allocate device memory (a host whose own pool owns the whole
+   device, or work issued where a cudaMalloc could synchronise the device).
+   Its scratch is a fixed device array of 3 x TG_NOALLOC_MAX_CELLS floats
+   held by every GPU that loads the library; larger grids are rejected with
+   TG_ERR_ARG. The first call on a device looks the array up (make it before
+   any stream capture); calls that overlap on the GPU race on the shared
+   scratch. `stream` is a cudaStream_t (NULL: the default stream). Errors
+   are described by tg_last_error(NULL). */
+#define TG_NOALLOC_MAX_CELLS 1310720
+int tg_filter_noalloc(int32_t dims, int32_t mx, int32_t my, int32_t mz, int32_t nghost, int32_t nghostz,
+                      const int32_t *periodic, int32_t ntimes, float *curx, float *cury, float *curz,
+                      void *stream);
+
 /* Wait for all work on the context's stream; returns any device status. */
 int tg_synchronize(tg_ctx *ctx);
 /* Current particle counts per species (synchronises). */

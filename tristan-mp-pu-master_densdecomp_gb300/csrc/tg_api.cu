@@ -320,6 +320,9 @@ extern "C" void tg_finalize(tg_ctx *ctx) {
 
 extern "C" const char *tg_last_error(tg_ctx *ctx) { return ctx ? ctx->err : g_init_error; }
 
+// error text for entry points that have no context (tg_last_error(NULL))
+void tg::tg_set_global_error(const char *msg) { snprintf(g_init_error, sizeof g_init_error, "%s", msg); }
+
 extern "C" int tg_synchronize(tg_ctx *ctx) {
     if (!ctx) return TG_ERR_ARG;
     CK(cudaStreamSynchronize(ctx->st));

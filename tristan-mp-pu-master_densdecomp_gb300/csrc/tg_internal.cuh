@@ -365,6 +365,9 @@ cudaError_t launch_aos_to_soa(const Geom &g, const void *in, const Species &sp, 
                               cudaStream_t st);
 cudaError_t launch_soa_to_aos(const Geom &g, const Species &sp, void *out, long long count, cudaStream_t st);
 
+// error text readable through tg_last_error(NULL) (tg_api.cu)
+void tg_set_global_error(const char *msg);
+
 // FP64 diagnostics (tg_diag.cu)
 struct DiagLaunch {
     Geom g;

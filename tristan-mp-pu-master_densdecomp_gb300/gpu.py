@@ -78,7 +78,7 @@ ENTRY_POINTS = (
     "tg_advance_e", "tg_move", "tg_reset_currents", "tg_deposit", "tg_fold_currents",
     "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_diag_fp64", "tg_synchronize",
     "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step", "tg_diag_history",
-    "tg_enable_timing", "tg_phase_times", "tg_step_timed",
+    "tg_enable_timing", "tg_phase_times", "tg_step_timed", "tg_filter_noalloc",
 )
 PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
