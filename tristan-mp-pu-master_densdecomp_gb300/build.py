@@ -61,7 +61,8 @@ def build(verbose: bool = False, ptxas_v: bool = False) -> str:
         o = os.path.join(OBJDIR, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
-            cmd = [cc] + ARCH + NVFLAGS + (["-Xptxas", "-v"] if ptxas_v else []) + ["-c", s, "-o", o]
+            extra = os.environ.get("TG_NVCC_EXTRA", "").split()
+            cmd = [cc] + ARCH + NVFLAGS + extra + (["-Xptxas", "-v"] if ptxas_v else []) + ["-c", s, "-o", o]
             jobs.append(cmd)
 
     def run(cmd):

@@ -115,11 +115,13 @@ class SimConfig:
 
     @property
     def fx_shift(self) -> int:
-        """Fixed-point scale 2^fx_shift: one unit is 2^-32 of the largest
-        particle charge, so a cell can sum ~2^31 charges of current before
-        the int64 accumulator overflows."""
+        """Fixed-point scale 2^fx_shift: one unit is at most 2^-29 of the
+        largest particle charge (finer than FP32 rounding of a deposit
+        contribution), a single contribution stays below 2^30 units (so the
+        device converts it with an exact 32-bit conversion), and a cell can
+        sum ~2^33 full charges before the int64 accumulator overflows."""
         qmax = max(abs(self.qi), abs(self.qe))
-        return 32 - int(math.ceil(math.log2(qmax)))
+        return 30 - int(math.ceil(math.log2(qmax)))
 
     def window_in(self):
         """x1in..z2in of allocate_particles (code/particles.F90:335-340);

@@ -63,7 +63,8 @@ struct tg_ctx {
     std::vector<cudaEvent_t> ev;
     int ev_laps = 0;
     int last_laps = 0;       // laps covered by the last launch (graph or direct)
-    bool ev_used[64][TG_NPHASES] = {};
+    bool last_direct = false;  // last lap ran outside the graph (event row ev_laps)
+    bool ev_used[65][TG_NPHASES] = {};
     long long lap = 0;
     long long lapreorder = 0;
     char err[512] = {0};
@@ -175,7 +176,7 @@ static int setup_geom(tg_ctx *ctx) {
     g.wy = ty + g.wlo + g.whi;
     g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
     g.wcells = g.wx * g.wy * g.wz;
-    const size_t smem = (size_t)3 * g.wcells * (c.deposit_mode == TG_DEPOSIT_FIXED ? 8 : 4);
+    const size_t smem = (size_t)6 * g.wcells * 4;
     if (smem > 227 * 1024)
         return fail(ctx, TG_ERR_ARG, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
     return TG_OK;
@@ -697,7 +698,7 @@ extern "C" int tg_diag_history(tg_ctx *ctx, double *out, int32_t n) {
 // fused lap
 // ---------------------------------------------------------------------------
 static cudaError_t mark(tg_ctx *ctx, int li, int phase, int end) {
-    if (!ctx->timing || li >= ctx->ev_laps) return cudaSuccess;
+    if (!ctx->timing || li > ctx->ev_laps) return cudaSuccess;
     if (!end) ctx->ev_used[li][phase] = true;
     return cudaEventRecord(ctx->ev[((size_t)li * TG_NPHASES + phase) * 2 + end], ctx->st);
 }
@@ -765,7 +766,8 @@ static int capture_cycle(tg_ctx *ctx, int start_par) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     int r = TG_OK, nk = 0;
-    for (int l = 0; l < 2 * se && r == TG_OK; l++) r = lap_kernels(ctx, (l % se) == se - 1, &nk, l);
+    for (int l = 0; l < 2 * se && r == TG_OK; l++)
+        r = lap_kernels(ctx, (l % se) == se - 1, &nk, l < ctx->ev_laps ? l : 1 << 20);
     cudaError_t e = cudaStreamEndCapture(ctx->st, &graph);
     if (r) {
         if (graph) cudaGraphDestroy(graph);
@@ -793,7 +795,10 @@ extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
     // cycle is tracked by the lap counter
     while (left > 0) {
         const int phase = (int)(ctx->lap % cyc);
-        if (phase == 0 && left >= cyc) {
+        // with timing on, the last lap always runs outside the graph: CUDA
+        // events recorded by graph nodes cannot be read back for elapsed time
+        const bool keep_last_direct = ctx->timing && left == cyc;
+        if (phase == 0 && left >= cyc && !keep_last_direct) {
             const int p = ctx->par;
             if (!ctx->cycle[p]) {
                 if ((r = capture_cycle(ctx, p))) return r;
@@ -803,10 +808,13 @@ extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
             ctx->lap += cyc;
             left -= cyc;
             ctx->last_laps = cyc;
+            ctx->last_direct = false;
         } else {
             int nk = 0;
-            if ((r = lap_kernels(ctx, (phase % se) == se - 1, &nk, 0))) return r;
+            // laps outside the graph time into their own event row
+            if ((r = lap_kernels(ctx, (phase % se) == se - 1, &nk, ctx->ev_laps))) return r;
             ctx->last_laps = 1;
+            ctx->last_direct = true;
             ctx->kernels_per_step = nk;
             ctx->lap += 1;
             left -= 1;
@@ -844,7 +852,7 @@ extern "C" int tg_enable_timing(tg_ctx *ctx, int32_t on) {
     if (on && ctx->ev.empty()) {
         const int se = ctx->cfg.sort_every < 1 ? 1 : ctx->cfg.sort_every;
         ctx->ev_laps = 2 * se < 64 ? 2 * se : 64;
-        ctx->ev.resize((size_t)ctx->ev_laps * TG_NPHASES * 2);
+        ctx->ev.resize((size_t)(ctx->ev_laps + 1) * TG_NPHASES * 2);
         for (auto &e : ctx->ev) CK(cudaEventCreate(&e));
     }
     ctx->timing = on != 0;
@@ -856,10 +864,11 @@ extern "C" int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases) {
     if (!ctx || !ms) return TG_ERR_ARG;
     if (!ctx->timing) return fail(ctx, TG_ERR_STATE, "tg_phase_times: timing not enabled");
     CK(cudaStreamSynchronize(ctx->st));
-    const int laps = ctx->last_laps < ctx->ev_laps ? ctx->last_laps : ctx->ev_laps;
+    const int laps = ctx->last_direct ? 1 : (ctx->last_laps < ctx->ev_laps ? ctx->last_laps : ctx->ev_laps);
+    const int row0 = ctx->last_direct ? ctx->ev_laps : 0;
     for (int ph = 0; ph < nphases && ph < TG_NPHASES; ph++) {
         float sum = 0.0f;
-        for (int li = 0; li < laps; li++) {
+        for (int li = row0; li < row0 + laps; li++) {
             if (!ctx->ev_used[li][ph]) continue;
             float t = 0.0f;
             const size_t b = ((size_t)li * TG_NPHASES + ph) * 2;

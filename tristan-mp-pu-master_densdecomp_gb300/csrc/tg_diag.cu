@@ -73,7 +73,8 @@ template <int DIM, int ORDER>
 __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
     constexpr int NS = ShapeN<ORDER>::NS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    unsigned long long *win = reinterpret_cast<unsigned long long *>(smem_raw);
+    unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
+    int *winhi = reinterpret_cast<int *>(smem_raw) + a.g.wcells;
     const Geom &g = a.g;
     const int tile = blockIdx.x;
     const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
@@ -81,13 +82,20 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
     const int wz0 = DIM == 3 ? g.oz + tiz * g.tz - g.wlo : 1;
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
     const int lox = g.ng / 2 + 1, loz = g.ngz / 2 + 1;
-    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) win[t] = 0ull;
+    for (int t = threadIdx.x; t < 2 * g.wcells; t += blockDim.x) winlo[t] = 0u;
     __syncthreads();
-    double part[7] = {0, 0, 0, 0, 0, 0, 0};  // eki, eke, px, py, pz, pad
+    double part[5] = {0, 0, 0, 0, 0};  // eki, eke, px, py, pz
+    // the window is exact for up to 65536 contributions per node: a denser
+    // tile deposits straight to global memory
+    const bool use_win = (a.tstart[0][tile + 1] - a.tstart[0][tile]) + (a.tstart[1][tile + 1] - a.tstart[1][tile]) <=
+                         TG_WIN_BATCH;
     for (int s = 0; s < 2; s++) {
         const Species sp = a.sp[s];
         const int beg = a.tstart[s][tile], end = a.tstart[s][tile + 1];
         const float qs = a.P.qs[s], m = a.mass[s];
+        // per-thread compensated FP32 sums, one FP64 add per thread and species
+        // (GB300 issues FP64 at a small fraction of the FP32 rate)
+        float ks[4] = {0, 0, 0, 0}, kc[4] = {0, 0, 0, 0};
         for (int n = beg + threadIdx.x; n < end; n += blockDim.x) {
             const int cell = sp.cell[n];
             if (cell < 0) continue;
@@ -111,12 +119,13 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
 #pragma unroll
                     for (int aa = 0; aa < NS; aa++) {
                         const float v = qyz * wx[aa];
-                        const long long fxv = __float2ll_rn(v * a.P.fx_scale);
+                        const float xs = v * a.P.fx_scale;
+                        const long long fxv = to_fixed(xs);
                         const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
                         const int ra = ii - wx0, rb = jj - wy0, rc = kk - wz0;
-                        if ((unsigned)ra < (unsigned)g.wx && (unsigned)rb < (unsigned)g.wy &&
-                            (unsigned)rc < (unsigned)g.wz) {
-                            atomicAdd(&win[ra + g.wx * (rb + g.wy * rc)], (unsigned long long)fxv);
+                        if (use_win && fabsf(xs) < 1073741824.0f && (unsigned)ra < (unsigned)g.wx &&
+                            (unsigned)rb < (unsigned)g.wy && (unsigned)rc < (unsigned)g.wz) {
+                            fx_add_shared(winlo, winhi, ra + g.wx * (rb + g.wy * rc), fxv);
                         } else {
                             const long long l = wrap_i(ii, lox, nx) +
                                                 (long long)nx * (wrap_i(jj, lox, ny) +
@@ -130,15 +139,23 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
             const float u2 = u * u + v * v + w * w;
             const float gm1 = u2 / (sqrtf(1.0f + u2) + 1.0f);
             const float mc = m * sp.ch[n];
-            part[s] += (double)(gm1 * mc);
-            part[2] += (double)(mc * u);
-            part[3] += (double)(mc * v);
-            part[4] += (double)(mc * w);
+            const float terms[4] = {gm1 * mc, mc * u, mc * v, mc * w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {  // Kahan summation
+                const float y = terms[q] - kc[q];
+                const float t = ks[q] + y;
+                kc[q] = (t - ks[q]) - y;
+                ks[q] = t;
+            }
         }
+        part[s] += (double)ks[0] - (double)kc[0];
+        part[2] += (double)ks[1] - (double)kc[1];
+        part[3] += (double)ks[2] - (double)kc[2];
+        part[4] += (double)ks[3] - (double)kc[3];
     }
     __syncthreads();
     for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
-        const unsigned long long val = win[t];
+        const unsigned long long val = (unsigned long long)fx_read_shared(winlo, winhi, t);
         if (val == 0ull) continue;
         const int ra = t % g.wx, rb = (t / g.wx) % g.wy, rc = t / (g.wx * g.wy);
         const long long l = wrap_i(wx0 + ra, lox, nx) +

@@ -155,6 +155,30 @@ __device__ __forceinline__ float pick(const float *w, int s, int off) {
     return r;
 }
 
+// float -> fixed point for values known to be below 2^30 in magnitude (the
+// deposit scale guarantees it for every contribution up to |q|); saturates
+// otherwise and flags nothing: callers that cannot guarantee the bound use
+// to_fixed
+__device__ __forceinline__ long long to_fixed32(float x) { return (long long)__float2int_rn(x); }
+
+// float -> int64 fixed point, round to nearest even (identical to llrintf);
+// the int32 conversion is exact and cheap whenever the value fits
+__device__ __forceinline__ long long to_fixed(float x) {
+    if (fabsf(x) < 2147483520.0f) return (long long)__float2int_rn(x);
+    return __float2ll_rn(x);
+}
+
+// a[i] for a runtime i in [0, N) without dynamic register indexing (which
+// would spill the array to local memory): a chain of selects
+template <int N>
+__device__ __forceinline__ float sel(const float *a, int i) {
+    float r = a[0];
+#pragma unroll
+    for (int k = 1; k < N; k++)
+        if (i == k) r = a[k];
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Fields seen by the particle kernels
 // ---------------------------------------------------------------------------
@@ -214,17 +238,18 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
     }
     float ex0 = 0.0f, ey0 = 0.0f, ez0 = 0.0f, bx0 = 0.0f, by0 = 0.0f, bz0 = 0.0f;
     if (DIM == 3) {
-#pragma unroll
+        // planes rolled (code size), rows and columns unrolled
+#pragma unroll 1
         for (int r3 = 0; r3 < NS; r3++) {
+            const float az = sel<NS>(azp, r3);
 #pragma unroll
             for (int r2 = 0; r2 < NS; r2++) {
-                const long long row = (long long)(ip - 3 + bxd - 1) +
-                                      g.sy * (long long)(jp - 3 + byd + r2 - 1) +
-                                      g.sz * (long long)(kp - 3 + bzd + r3 - 1);
+                const int row = (ip - 3 + bxd - 1) + (int)g.sy * (jp - 3 + byd + r2 - 1) +
+                                (int)g.sz * (kp - 3 + bzd + r3 - 1);
                 float sx = 0.0f, sy = 0.0f, sz = 0.0f, sbx = 0.0f, sby = 0.0f, sbz = 0.0f;
 #pragma unroll
                 for (int r1 = 0; r1 < NS; r1++) {
-                    const long long l = row + r1;
+                    const int l = row + r1;
                     sx = sx + __ldg(f.pex + l) * axp[r1];
                     sy = sy + __ldg(f.pey + l) * axp[r1];
                     sz = sz + __ldg(f.pez + l) * axp[r1];
@@ -232,30 +257,32 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
                     sby = sby + __ldg(f.pby + l) * axp[r1];
                     sbz = sbz + __ldg(f.pbz + l) * axp[r1];
                 }
-                ex0 = ex0 + sx * ayp[r2] * azp[r3];
-                ey0 = ey0 + sy * ayp[r2] * azp[r3];
-                ez0 = ez0 + sz * ayp[r2] * azp[r3];
-                bx0 = bx0 + sbx * ayp[r2] * azp[r3];
-                by0 = by0 + sby * ayp[r2] * azp[r3];
-                bz0 = bz0 + sbz * ayp[r2] * azp[r3];
+                ex0 = ex0 + sx * ayp[r2] * az;
+                ey0 = ey0 + sy * ayp[r2] * az;
+                ez0 = ez0 + sz * ayp[r2] * az;
+                bx0 = bx0 + sbx * ayp[r2] * az;
+                by0 = by0 + sby * ayp[r2] * az;
+                bz0 = bz0 + sbz * ayp[r2] * az;
             }
         }
     } else {
-#pragma unroll
+        // rows rolled (code size), columns unrolled
+#pragma unroll 1
         for (int r2 = 0; r2 < NS; r2++) {
-            const long long rowp = g.sy * (long long)(jp - 3 + byd + r2 - 1);
-            const long long rowd = g.sy * (long long)(jd - 3 + byd + r2 - 1);
+            const int rowp = (int)g.sy * (jp - 3 + byd + r2 - 1);
+            const int rowd = (int)g.sy * (jd - 3 + byd + r2 - 1);
+            const float ay = sel<NS>(ayp, r2), wy = sel<NS>(wyd, r2);
 #pragma unroll
             for (int r1 = 0; r1 < NS; r1++) {
-                const long long colp = (long long)(ip - 3 + bxd + r1 - 1);
-                const long long cold = (long long)(id - 3 + bxd + r1 - 1);
-                const long long lpp = colp + rowp, lpd = colp + rowd, ldp = cold + rowp, ldd = cold + rowd;
-                ex0 = ex0 + __ldg(f.ex + ldp) * wxd[r1] * ayp[r2];
-                ey0 = ey0 + __ldg(f.ey + lpd) * axp[r1] * wyd[r2];
-                ez0 = ez0 + __ldg(f.ez + lpp) * axp[r1] * ayp[r2];
-                bx0 = bx0 + __ldg(f.bx + lpd) * axp[r1] * wyd[r2];
-                by0 = by0 + __ldg(f.by + ldp) * wxd[r1] * ayp[r2];
-                bz0 = bz0 + __ldg(f.bz + ldd) * wxd[r1] * wyd[r2];
+                const int colp = ip - 3 + bxd + r1 - 1;
+                const int cold = id - 3 + bxd + r1 - 1;
+                const int lpp = colp + rowp, lpd = colp + rowd, ldp = cold + rowp, ldd = cold + rowd;
+                ex0 = ex0 + __ldg(f.ex + ldp) * wxd[r1] * ay;
+                ey0 = ey0 + __ldg(f.ey + lpd) * axp[r1] * wy;
+                ez0 = ez0 + __ldg(f.ez + lpp) * axp[r1] * ay;
+                bx0 = bx0 + __ldg(f.bx + lpd) * axp[r1] * wy;
+                by0 = by0 + __ldg(f.by + ldp) * wxd[r1] * ay;
+                bz0 = bz0 + __ldg(f.bz + ldd) * wxd[r1] * wy;
             }
         }
     }

@@ -92,10 +92,29 @@ __device__ __forceinline__ int agg_inc(int *counter, int key) {
 // ---------------------------------------------------------------------------
 // Deposit sinks
 // ---------------------------------------------------------------------------
+// Shared-memory deposit window in exact fixed point. A contribution
+// q (|q| < 2^31 units) is split into q = qh*2^16 + ql, ql in [0, 2^16), and
+// the two parts go into two 32-bit accumulators with native, non-returning
+// 32-bit shared atomic adds (FP32 shared atomics are compare-and-swap loops
+// on this GPU: a load, an add, a CAS and a branch per update). Exact for up to
+// 65536 contributions per cell and tile: the low sums stay below 2^32 and the
+// high sums inside int32. Value = hi * 2^16 + lo.
+__device__ __forceinline__ void fx_add_shared(unsigned *lo, int *hi, int idx, long long q) {
+    const int q32 = (int)q;  // callers guarantee |q| < 2^31
+    atomicAdd(lo + idx, (unsigned)(q32 & 0xffff));
+    const int qh = q32 >> 16;  // arithmetic shift: floor division by 2^16
+    if (qh != 0) atomicAdd(hi + idx, qh);
+}
+
+__device__ __forceinline__ long long fx_read_shared(const unsigned *lo, const int *hi, int idx) {
+    return (long long)hi[idx] * 65536LL + (long long)lo[idx];
+}
+
 template <bool FIXED>
 struct WindowSink {
-    typedef typename std::conditional<FIXED, unsigned long long, float>::type T;
-    T *s;  // [3][wcells]
+    float *s;        // FP32 mode: [3][wcells]
+    unsigned *lo;    // fixed point: low words [3][wcells]
+    int *hi;         // fixed point: high words [3][wcells]
     int wx0, wy0, wz0, wx, wy, wz, wcells;
     float *gc[3];
     unsigned long long *gf[3];
@@ -106,25 +125,25 @@ struct WindowSink {
         const int a = i - wx0, b = j - wy0, c = k - wz0;
         if ((unsigned)a < (unsigned)wx && (unsigned)b < (unsigned)wy && (unsigned)c < (unsigned)wz) {
             const int idx = comp * wcells + a + wx * (b + wy * c);
-            if (FIXED) {
-                long long q = __float2ll_rn(v * scale);
-                atomicAdd((unsigned long long *)&s[idx], (unsigned long long)q);
-            } else {
-                atomicAdd((float *)&s[idx], v);
+            if (!FIXED) {
+                atomicAdd(s + idx, v);
+                return;
             }
-        } else {
+            const float x = v * scale;
+            if (fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact split path
+                fx_add_shared(lo, hi, idx, to_fixed32(x));
+                return;
+            }
+        }
+        {
             // outside the tile window: straight to global memory
             if (i < 1 || i > g->mx || j < 1 || j > g->my || k < 1 || k > g->mz) {
                 atomicOr(status, ST_BOUNDS);
                 return;
             }
-            const long long l = lin(*g, i, j, k);
-            if (FIXED) {
-                long long q = __float2ll_rn(v * scale);
-                atomicAdd(gf[comp] + l, (unsigned long long)q);
-            } else {
-                atomicAdd(gc[comp] + l, v);
-            }
+            const int l = (i - 1) + (int)g->sy * ((j - 1) + g->my * (k - 1));
+            if (FIXED) atomicAdd(gf[comp] + l, (unsigned long long)to_fixed(v * scale));
+            else atomicAdd(gc[comp] + l, v);
         }
     }
 };
@@ -177,10 +196,11 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
 
     if (DIM == 2) {
         const float deltaz = z2 - z1;
-#pragma unroll
-        for (int ry = 0; ry < U; ry++) {
-            if (ry < ny) {
-                const float s1y = S1y[ry], dSy = S2y[ry] - S1y[ry];
+        // rows rolled (code size), the row's cells unrolled (carries in registers)
+#pragma unroll 1
+        for (int ry = 0; ry < ny; ry++) {
+            {
+                const float s1y = sel<U>(S1y, ry), dSy = sel<U>(S2y, ry) - s1y;
                 const float wy = s1y + TG_HALF * dSy;
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
@@ -226,11 +246,18 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
         for (int rx = 0; rx < U; rx++)
 #pragma unroll
             for (int ry = 0; ry < U; ry++) czp[rx][ry] = 0.0f;
+        float S1z[U], S2z[U];
 #pragma unroll
-        for (int rz = 0; rz < U; rz++) {
-            if (rz < nz) {
-                const float s1z = pick<NS>(w1z, rz, b1z - loz);
-                const float dSz = pick<NS>(w2z, rz, b2z - loz) - s1z;
+        for (int r = 0; r < U; r++) {
+            S1z[r] = pick<NS>(w1z, r, b1z - loz);
+            S2z[r] = pick<NS>(w2z, r, b2z - loz);
+        }
+        // planes rolled (code size), each plane's cells unrolled
+#pragma unroll 1
+        for (int rz = 0; rz < nz; rz++) {
+            {
+                const float s1z = sel<U>(S1z, rz);
+                const float dSz = sel<U>(S2z, rz) - s1z;
                 float wxz[U];
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
@@ -268,16 +295,64 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
 // ---------------------------------------------------------------------------
 // The tile kernel
 // ---------------------------------------------------------------------------
+#define TG_WIN_BATCH 65536
+
+// add the window sums to the global currents: fixed point keeps exact int64
+// sums across tiles; the FP32 mode adds its FP32 tile sums with FP32 atomics
+template <bool FIXED>
+__device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink<FIXED> &sink, const unsigned *winlo,
+                                             const int *winhi) {
+    const float *winf = reinterpret_cast<const float *>(winlo);
+    const Geom &g = a.g;
+    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
+        const int a0 = t % g.wx, b0 = (t / g.wx) % g.wy, c0 = t / (g.wx * g.wy);
+        const int i = sink.wx0 + a0, j = sink.wy0 + b0, k = sink.wz0 + c0;
+        const bool inside = i >= 1 && i <= g.mx && j >= 1 && j <= g.my && k >= 1 && k <= g.mz;
+        const long long l = inside ? lin(g, i, j, k) : 0;
+#pragma unroll
+        for (int cc = 0; cc < 3; cc++) {
+            if (FIXED) {
+                const long long val = fx_read_shared(winlo, winhi, cc * g.wcells + t);
+                if (val == 0) continue;
+                if (!inside) {
+                    atomicOr(a.status, ST_BOUNDS);
+                    continue;
+                }
+                atomicAdd(a.fix[cc] + l, (unsigned long long)val);
+            } else {
+                const float val = winf[cc * g.wcells + t];
+                if (val == 0.0f) continue;
+                if (!inside) {
+                    atomicOr(a.status, ST_BOUNDS);
+                    continue;
+                }
+                atomicAdd(a.cur[cc] + l, val);
+            }
+        }
+    }
+}
+
+// resident CTAs per SM the register budget is sized for: 2D kernels run
+// best at 4 (64 registers, small spills), 3D kernels carry more state
+#ifndef TG_TILES_MINB_2D
+#define TG_TILES_MINB_2D 4
+#endif
+#ifndef TG_TILES_MINB_3D
+#define TG_TILES_MINB_3D 2
+#endif
 template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
-__global__ void __launch_bounds__(256) k_tiles(TileArgs a) {
-    typedef typename WindowSink<FIXED>::T T;
+__global__ void __launch_bounds__(256, DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MINB_2D) k_tiles(TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *win = reinterpret_cast<T *>(smem_raw);
+    unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
+    int *winhi = reinterpret_cast<int *>(smem_raw) + 3 * a.g.wcells;
+    float *winf = reinterpret_cast<float *>(smem_raw);
     const Geom &g = a.g;
     const int tile = blockIdx.x;
     const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
     WindowSink<FIXED> sink;
-    sink.s = win;
+    sink.s = winf;
+    sink.lo = winlo;
+    sink.hi = winhi;
     sink.wx0 = g.ox + tix * g.tx - g.wlo;
     sink.wy0 = g.oy + tiy * g.ty - g.wlo;
     sink.wz0 = DIM == 3 ? g.oz + tiz * g.tz - g.wlo : 1;
@@ -292,10 +367,15 @@ __global__ void __launch_bounds__(256) k_tiles(TileArgs a) {
     sink.scale = a.P.fx_scale;
     sink.g = &a.g;
     sink.status = a.status;
+    const int nwords = (FIXED ? 6 : 3) * g.wcells;
     if (DEPOSIT) {
-        for (int t = threadIdx.x; t < 3 * g.wcells; t += blockDim.x) win[t] = (T)0;
+        for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
         __syncthreads();
     }
+    // particles since the last flush; the window is exact for up to 65536
+    // contributions per cell, i.e. 65536 particles (every bound is uniform
+    // across the CTA, so the barriers below are reached by all threads)
+    int since = 0;
 #pragma unroll 1
     for (int s = 0; s < 2; s++) {
         const Species sp = a.sp[s];
@@ -303,69 +383,66 @@ __global__ void __launch_bounds__(256) k_tiles(TileArgs a) {
         const float qm = a.P.qm[s];
         const float qs = a.P.qs[s];
 #pragma unroll 1
-        for (int n = beg + threadIdx.x; n < end; n += blockDim.x) {
-            if (sp.cell[n] < 0) continue;  // discarded since the last sort
-            float x, y, z;
-            load_pos<DIM>(g, sp, n, x, y, z);
-            float u = sp.u[n], v = sp.v[n], w = sp.w[n];
-            if (PUSH) {
-                if (!gather_safe<DIM>(g, x, y, z)) {
-                    atomicOr(a.status, ST_BOUNDS);
-                    sp.cell[n] = -1;
-                    continue;
+        for (int b0 = beg; b0 < end;) {
+            const int b1 = min(end, b0 + (TG_WIN_BATCH - since));
+#pragma unroll 1
+            for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x) {
+                if (sp.cell[n] < 0) continue;  // discarded since the last sort
+                float x, y, z;
+                load_pos<DIM>(g, sp, n, x, y, z);
+                float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+                if (PUSH) {
+                    if (!gather_safe<DIM>(g, x, y, z)) {
+                        atomicOr(a.status, ST_BOUNDS);
+                        sp.cell[n] = -1;
+                        continue;
+                    }
+                    push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
                 }
-                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
+                bool keep = true;
+                if (DEPOSIT) {
+                    // reconstruct the previous position from the new momentum
+                    // (deposit_particles, code/particles_movedeposit.F90:1384-1390)
+                    const float c = a.P.c;
+                    const float invgam = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
+                    const float x0 = x - u * invgam * c;
+                    const float y0 = y - v * invgam * c;
+                    const float z0 = z - w * invgam * c;
+                    const float q = sp.ch[n] * qs;
+                    esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
+                    keep = wrap_particle<DIM>(g, a.P, x, y, z);
+                }
+                int i, j, k;
+                const bool fin = isfinite(x) && isfinite(y) && isfinite(z);
+                if (!fin) atomicOr(a.status, ST_NAN);
+                if (keep && fin && pos_cell<DIM>(g, x, y, z, i, j, k)) {
+                    store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
+                    if (a.newcount[s]) agg_inc(a.newcount[s], tile_of(g, i, j, k));
+                } else {
+                    if (keep) atomicOr(a.status, ST_BOUNDS);
+                    sp.cell[n] = -1;  // discarded: dropped by the next sort
+                }
+                if (PUSH) {
+                    sp.u[n] = u;
+                    sp.v[n] = v;
+                    sp.w[n] = w;
+                }
             }
-            bool keep = true;
-            if (DEPOSIT) {
-                // reconstruct the previous position from the new momentum
-                // (deposit_particles, code/particles_movedeposit.F90:1384-1390)
-                const float c = a.P.c;
-                const float invgam = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
-                const float x0 = x - u * invgam * c;
-                const float y0 = y - v * invgam * c;
-                const float z0 = z - w * invgam * c;
-                const float q = sp.ch[n] * qs;
-                esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
-                keep = wrap_particle<DIM>(g, a.P, x, y, z);
-            }
-            int i, j, k;
-            const bool fin = isfinite(x) && isfinite(y) && isfinite(z);
-            if (!fin) atomicOr(a.status, ST_NAN);
-            if (keep && fin && pos_cell<DIM>(g, x, y, z, i, j, k)) {
-                store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
-                if (a.newcount[s]) agg_inc(a.newcount[s], tile_of(g, i, j, k));
-            } else {
-                if (keep) atomicOr(a.status, ST_BOUNDS);
-                sp.cell[n] = -1;  // discarded: dropped by the next sort
-            }
-            if (PUSH) {
-                sp.u[n] = u;
-                sp.v[n] = v;
-                sp.w[n] = w;
+            since += b1 - b0;
+            b0 = b1;
+            if (DEPOSIT && since == TG_WIN_BATCH) {
+                __syncthreads();
+                flush_window<FIXED>(a, sink, winlo, winhi);
+                __syncthreads();
+                for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
+                __syncthreads();
+                since = 0;
             }
         }
     }
-    if (DEPOSIT) {
+    if (DEPOSIT && since > 0) {
         __syncthreads();
-        for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
-            const int a0 = t % g.wx, b0 = (t / g.wx) % g.wy, c0 = t / (g.wx * g.wy);
-            const int i = sink.wx0 + a0, j = sink.wy0 + b0, k = sink.wz0 + c0;
-            const bool inside = i >= 1 && i <= g.mx && j >= 1 && j <= g.my && k >= 1 && k <= g.mz;
-            const long long l = inside ? lin(g, i, j, k) : 0;
-#pragma unroll
-            for (int cc = 0; cc < 3; cc++) {
-                const T val = win[cc * g.wcells + t];
-                if (val != (T)0) {
-                    if (!inside) {
-                        atomicOr(a.status, ST_BOUNDS);
-                        continue;
-                    }
-                    if (FIXED) atomicAdd(a.fix[cc] + l, (unsigned long long)val);
-                    else atomicAdd(a.cur[cc] + l, (float)val);
-                }
-            }
-        }
+        flush_window<FIXED>(a, sink, winlo, winhi);
     }
 }
 

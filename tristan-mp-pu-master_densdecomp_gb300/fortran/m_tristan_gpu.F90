@@ -171,7 +171,7 @@ contains
     cfg%x1in = x1in; cfg%x2in = x2in; cfg%y1in = y1in; cfg%y2in = y2in; cfg%z1in = z1in; cfg%z2in = z2in
     cfg%mxcum = mxcum; cfg%mycum = mycum; cfg%mzcum = mzcum
     cfg%deposit_mode = deposit_mode
-    cfg%fx_shift = 32 - ceiling(log(max(abs(qi), abs(qe))) / log(2.))
+    cfg%fx_shift = 30 - ceiling(log(max(abs(qi), abs(qe))) / log(2.))
     cfg%maxhlf = maxhlf
     cfg%sort_every = sort_every
     cfg%tile = 0; cfg%device = 0; cfg%diag_every = 0

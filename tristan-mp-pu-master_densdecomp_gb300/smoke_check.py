@@ -2,8 +2,8 @@
 
 A 2D order-3 box of 48 x 32 cells with two counter-streaming pair beams
 (4 per cell per species): one fixed-point lap must match the oracle bit for
-bit (fields and particles), one FP32 lap within 1e-5 of each field's
-maximum. Raises on any mismatch or if the CUDA library is unavailable.
+bit (fields and particles), one FP32 lap within 1e-5 norm-wise relative
+error (1e-4 of the maximum element-wise). Raises on any mismatch or if the CUDA library is unavailable.
 """
 from __future__ import annotations
 
@@ -42,9 +42,10 @@ def _case(fixed: int):
                 if not np.array_equal(ref, got):
                     raise AssertionError(f"smoke: {k} differs from the oracle (fixed point)")
             else:
-                err = float(np.abs(got.astype(np.float64) - ref).max())
-                if err > 1e-5 * max(float(np.abs(ref).max()), 1e-30):
-                    raise AssertionError(f"smoke: {k} error {err:.3e} above tolerance")
+                d = got.astype(np.float64) - ref
+                rel = float(np.linalg.norm(d) / max(np.linalg.norm(ref), 1e-300))
+                if rel > 1e-5 or float(np.abs(d).max()) > 1e-4 * max(float(np.abs(ref).max()), 1e-30):
+                    raise AssertionError(f"smoke: {k} relative error {rel:.3e} above tolerance")
         a, b = np.sort(g.ions, order="ind"), np.sort(o.ions, order="ind")
         for k in ("x", "y", "z", "u", "v", "w"):
             if not np.array_equal(a[k], b[k]):
