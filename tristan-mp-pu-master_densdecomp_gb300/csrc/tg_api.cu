@@ -176,7 +176,7 @@ static int setup_geom(tg_ctx *ctx) {
     g.wy = ty + g.wlo + g.whi;
     g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
     g.wcells = g.wx * g.wy * g.wz;
-    const size_t smem = (size_t)6 * g.wcells * 4;
+    const size_t smem = (size_t)6 * g.wcells * 4;  // split 32-bit window, 3 components
     if (smem > 227 * 1024)
         return fail(ctx, TG_ERR_ARG, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
     return TG_OK;
@@ -639,7 +639,7 @@ extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
 // ---------------------------------------------------------------------------
 // FP64 diagnostics
 // ---------------------------------------------------------------------------
-static int run_diag(tg_ctx *ctx) {
+static int run_diag(tg_ctx *ctx, bool particles) {
     DiagLaunch d;
     memset(&d, 0, sizeof d);
     d.g = ctx->g;
@@ -659,6 +659,7 @@ static int run_diag(tg_ctx *ctx) {
     d.counter = ctx->dcounter;
     d.ntimes = ctx->cfg.ntimes;
     d.status = ctx->d_status;
+    d.particles = particles;
     CK(launch_diag(d, ctx->st));
     return TG_OK;
 }
@@ -752,7 +753,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
     }
     if (ctx->cfg.diag_every > 0) {
         CK(mark(ctx, li, 5, 0));
-        int rr = run_diag(ctx);
+        int rr = run_diag(ctx, true);
         if (rr) return rr;
         k += 4 + ctx->cfg.ntimes;
         CK(mark(ctx, li, 5, 1));
@@ -888,7 +889,7 @@ extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
     if (!ctx || !out) return TG_ERR_ARG;
     int r = ensure_sorted(ctx);
     if (r) return r;
-    if ((r = run_diag(ctx))) return r;
+    if ((r = run_diag(ctx, true))) return r;
     double h[16];
     if (tg_diag_history(ctx, h, 1) != 1) return fail(ctx, TG_ERR_STATE, "tg_diag_fp64: no record");
     record_to_diag(h, out);

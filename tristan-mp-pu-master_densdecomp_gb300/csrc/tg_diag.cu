@@ -22,35 +22,6 @@
 
 namespace tg {
 
-enum { D_RES2 = 0, D_RHO2, D_CHARGE, D_EE, D_EB, D_EKI, D_EKE, D_PX, D_PY, D_PZ, D_FX, D_FY, D_FZ, D_N = 16 };
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// block-reduce `vals[NV]` and add the block total to acc[first..]
-template <int NV>
-__device__ __forceinline__ void block_accumulate(double *vals, double *acc, int first) {
-    __shared__ double red[32][NV];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < NV; q++) vals[q] = warp_sum(vals[q]);
-    if (lane == 0)
-#pragma unroll
-        for (int q = 0; q < NV; q++) red[wid][q] = vals[q];
-    __syncthreads();
-    if (wid == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-        for (int q = 0; q < NV; q++) {
-            double v = lane < nw ? red[lane][q] : 0.0;
-            v = warp_sum(v);
-            if (lane == 0 && v != 0.0) atomicAdd(acc + first + q, v);
-        }
-    }
-}
 
 struct DiagArgs {
     Geom g;
@@ -63,15 +34,8 @@ struct DiagArgs {
     int *status;
 };
 
-__device__ __forceinline__ int wrap_i(int i, int lo, int n) {
-    int r = (i - lo) % n;
-    if (r < 0) r += n;
-    return r;
-}
-
 template <int DIM, int ORDER>
 __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
-    constexpr int NS = ShapeN<ORDER>::NS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
     int *winhi = reinterpret_cast<int *>(smem_raw) + a.g.wcells;
@@ -80,8 +44,6 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
     const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
     const int wx0 = g.ox + tix * g.tx - g.wlo, wy0 = g.oy + tiy * g.ty - g.wlo;
     const int wz0 = DIM == 3 ? g.oz + tiz * g.tz - g.wlo : 1;
-    const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
-    const int lox = g.ng / 2 + 1, loz = g.ngz / 2 + 1;
     for (int t = threadIdx.x; t < 2 * g.wcells; t += blockDim.x) winlo[t] = 0u;
     __syncthreads();
     double part[5] = {0, 0, 0, 0, 0};  // eki, eke, px, py, pz
@@ -104,37 +66,8 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
             const float ox = sp.ox[n], oy = sp.oy[n];
             const float oz = DIM == 3 ? sp.oz[n] : 0.0f;
             const float q = sp.ch[n] * qs;
-            float wx[NS], wy[NS], wz[NS];
-            int bx, by, bz = 3;
-            shape<ORDER>(ox, wx, bx);
-            shape<ORDER>(oy, wy, by);
-            if (DIM == 3) shape<ORDER>(oz, wz, bz);
-            else wz[0] = 1.0f;
-            constexpr int NZ = DIM == 3 ? NS : 1;
-#pragma unroll
-            for (int c = 0; c < NZ; c++) {
-#pragma unroll
-                for (int b = 0; b < NS; b++) {
-                    const float qyz = q * wy[b] * wz[c];
-#pragma unroll
-                    for (int aa = 0; aa < NS; aa++) {
-                        const float v = qyz * wx[aa];
-                        const float xs = v * a.P.fx_scale;
-                        const long long fxv = to_fixed(xs);
-                        const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
-                        const int ra = ii - wx0, rb = jj - wy0, rc = kk - wz0;
-                        if (use_win && fabsf(xs) < 1073741824.0f && (unsigned)ra < (unsigned)g.wx &&
-                            (unsigned)rb < (unsigned)g.wy && (unsigned)rc < (unsigned)g.wz) {
-                            fx_add_shared(winlo, winhi, ra + g.wx * (rb + g.wy * rc), fxv);
-                        } else {
-                            const long long l = wrap_i(ii, lox, nx) +
-                                                (long long)nx * (wrap_i(jj, lox, ny) +
-                                                                 (long long)ny * (DIM == 3 ? wrap_i(kk, loz, nz) : 0));
-                            atomicAdd(a.rhofx + l, (unsigned long long)fxv);
-                        }
-                    }
-                }
-            }
+            rho_deposit<DIM, ORDER>(g, a.P.fx_scale, i, j, k, ox, oy, oz, q, winlo, winhi, wx0, wy0, wz0, use_win,
+                                    a.rhofx);
             const float u = sp.u[n], v = sp.v[n], w = sp.w[n];
             const float u2 = u * u + v * v + w * w;
             const float gm1 = u2 / (sqrtf(1.0f + u2) + 1.0f);
@@ -154,15 +87,7 @@ __global__ void __launch_bounds__(256) k_diag_particles(DiagArgs a) {
         part[4] += (double)ks[3] - (double)kc[3];
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
-        const unsigned long long val = (unsigned long long)fx_read_shared(winlo, winhi, t);
-        if (val == 0ull) continue;
-        const int ra = t % g.wx, rb = (t / g.wx) % g.wy, rc = t / (g.wx * g.wy);
-        const long long l = wrap_i(wx0 + ra, lox, nx) +
-                            (long long)nx * (wrap_i(wy0 + rb, lox, ny) +
-                                             (long long)ny * (DIM == 3 ? wrap_i(wz0 + rc, loz, nz) : 0));
-        atomicAdd(a.rhofx + l, val);
-    }
+    rho_flush<DIM>(g, winlo, winhi, wx0, wy0, wz0, a.rhofx);
     block_accumulate<5>(part, a.acc, D_EKI);
 }
 
@@ -279,7 +204,7 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
     a.acc = d.acc;
     a.status = d.status;
     const size_t smem = (size_t)g.wcells * 8;
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
 #define TG_DL(D, O)                                                                                     \
     do {                                                                                                \
         e = cudaFuncSetAttribute(k_diag_particles<D, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
@@ -287,7 +212,8 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
         if (e != cudaSuccess) return e;                                                                 \
         k_diag_particles<D, O><<<g.ntiles, 256, smem, st>>>(a);                                         \
     } while (0)
-    if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
+    if (!d.particles) {
+    } else if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
     else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
     else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
     else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);

@@ -411,6 +411,7 @@ struct DiagLaunch {
     unsigned long long *counter;
     int ntimes;
     int *status;
+    bool particles;  // false: the lap's tile kernel already summed the particles
 };
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
 

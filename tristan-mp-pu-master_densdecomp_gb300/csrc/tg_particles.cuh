@@ -89,6 +89,37 @@ __device__ __forceinline__ int agg_inc(int *counter, int key) {
     return base + __popc(peers & ((1u << lane) - 1u));
 }
 
+// FP64 block reductions for the diagnostics accumulators
+enum { D_RES2 = 0, D_RHO2, D_CHARGE, D_EE, D_EB, D_EKI, D_EKE, D_PX, D_PY, D_PZ, D_FX, D_FY, D_FZ, D_N = 16 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-reduce `vals[NV]` and add the block total to acc[first..]
+template <int NV>
+__device__ __forceinline__ void block_accumulate(double *vals, double *acc, int first) {
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) vals[q] = warp_sum(vals[q]);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) red[wid][q] = vals[q];
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double v = lane < nw ? red[lane][q] : 0.0;
+            v = warp_sum(v);
+            if (lane == 0 && v != 0.0) atomicAdd(acc + first + q, v);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Deposit sinks
 // ---------------------------------------------------------------------------
@@ -112,9 +143,8 @@ __device__ __forceinline__ long long fx_read_shared(const unsigned *lo, const in
 
 template <bool FIXED>
 struct WindowSink {
-    float *s;        // FP32 mode: [3][wcells]
-    unsigned *lo;    // fixed point: low words [3][wcells]
-    int *hi;         // fixed point: high words [3][wcells]
+    unsigned *lo;    // low words [3][wcells]
+    int *hi;         // high words [3][wcells]
     int wx0, wy0, wz0, wx, wy, wz, wcells;
     float *gc[3];
     unsigned long long *gf[3];
@@ -125,10 +155,6 @@ struct WindowSink {
         const int a = i - wx0, b = j - wy0, c = k - wz0;
         if ((unsigned)a < (unsigned)wx && (unsigned)b < (unsigned)wy && (unsigned)c < (unsigned)wz) {
             const int idx = comp * wcells + a + wx * (b + wy * c);
-            if (!FIXED) {
-                atomicAdd(s + idx, v);
-                return;
-            }
             const float x = v * scale;
             if (fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact split path
                 fx_add_shared(lo, hi, idx, to_fixed32(x));
@@ -297,12 +323,74 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
 // ---------------------------------------------------------------------------
 #define TG_WIN_BATCH 65536
 
-// add the window sums to the global currents: fixed point keeps exact int64
-// sums across tiles; the FP32 mode adds its FP32 tile sums with FP32 atomics
+__device__ __forceinline__ int wrap_i(int i, int lo, int n) {
+    int r = (i - lo) % n;
+    if (r < 0) r += n;
+    return r;
+}
+
+// linear index of node (ii,jj,kk) folded into the periodic interior
+template <int DIM>
+__device__ __forceinline__ long long interior_index(const Geom &g, int ii, int jj, int kk) {
+    const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
+    const int lo = g.ng / 2 + 1, loz = g.ngz / 2 + 1;
+    return wrap_i(ii, lo, nx) + (long long)nx * (wrap_i(jj, lo, ny) + (long long)ny * (DIM == 3 ? wrap_i(kk, loz, nz) : 0));
+}
+
+// charge of one particle at node offsets (ox,oy,oz) of node (i,j,k), with
+// the deposit's B-spline: FP32 products, one rounding to fixed point, into
+// the shared window (wx0.. origin) or, outside it, the periodic interior
+template <int DIM, int ORDER>
+__device__ __forceinline__ void rho_deposit(const Geom &g, float fx_scale, int i, int j, int k, float ox, float oy,
+                                            float oz, float q, unsigned *rlo, int *rhi, int wx0, int wy0, int wz0,
+                                            bool use_win, unsigned long long *rhofx) {
+    constexpr int NS = ShapeN<ORDER>::NS;
+    float wx[NS], wy[NS], wz[NS];
+    int bx, by, bz = 3;
+    shape<ORDER>(ox, wx, bx);
+    shape<ORDER>(oy, wy, by);
+    if (DIM == 3) shape<ORDER>(oz, wz, bz);
+    else wz[0] = 1.0f;
+    constexpr int NZ = DIM == 3 ? NS : 1;
+#pragma unroll 1
+    for (int c = 0; c < NZ; c++) {
+        const float wzc = sel<NS>(wz, c);
+#pragma unroll
+        for (int b = 0; b < NS; b++) {
+            const float qyz = q * wy[b] * wzc;
+#pragma unroll
+            for (int aa = 0; aa < NS; aa++) {
+                const float xs = qyz * wx[aa] * fx_scale;
+                const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
+                const int ra = ii - wx0, rb = jj - wy0, rc = kk - wz0;
+                if (use_win && fabsf(xs) < 1073741824.0f && (unsigned)ra < (unsigned)g.wx &&
+                    (unsigned)rb < (unsigned)g.wy && (unsigned)rc < (unsigned)g.wz) {
+                    fx_add_shared(rlo, rhi, ra + g.wx * (rb + g.wy * rc), to_fixed32(xs));
+                } else {
+                    atomicAdd(rhofx + interior_index<DIM>(g, ii, jj, kk), (unsigned long long)to_fixed(xs));
+                }
+            }
+        }
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void rho_flush(const Geom &g, const unsigned *rlo, const int *rhi, int wx0, int wy0, int wz0,
+                                          unsigned long long *rhofx) {
+    for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
+        const long long val = fx_read_shared(rlo, rhi, t);
+        if (val == 0) continue;
+        const int ra = t % g.wx, rb = (t / g.wx) % g.wy, rc = t / (g.wx * g.wy);
+        atomicAdd(rhofx + interior_index<DIM>(g, wx0 + ra, wy0 + rb, wz0 + rc), (unsigned long long)val);
+    }
+}
+
+// add the exact window sums to the global currents: fixed point keeps int64
+// sums across tiles; the FP32 mode rounds each tile sum once and adds it
+// with FP32 global atomics (native on this GPU, unlike FP32 shared atomics)
 template <bool FIXED>
 __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink<FIXED> &sink, const unsigned *winlo,
                                              const int *winhi) {
-    const float *winf = reinterpret_cast<const float *>(winlo);
     const Geom &g = a.g;
     for (int t = threadIdx.x; t < g.wcells; t += blockDim.x) {
         const int a0 = t % g.wx, b0 = (t / g.wx) % g.wy, c0 = t / (g.wx * g.wy);
@@ -311,23 +399,14 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
         const long long l = inside ? lin(g, i, j, k) : 0;
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
-            if (FIXED) {
-                const long long val = fx_read_shared(winlo, winhi, cc * g.wcells + t);
-                if (val == 0) continue;
-                if (!inside) {
-                    atomicOr(a.status, ST_BOUNDS);
-                    continue;
-                }
-                atomicAdd(a.fix[cc] + l, (unsigned long long)val);
-            } else {
-                const float val = winf[cc * g.wcells + t];
-                if (val == 0.0f) continue;
-                if (!inside) {
-                    atomicOr(a.status, ST_BOUNDS);
-                    continue;
-                }
-                atomicAdd(a.cur[cc] + l, val);
+            const long long val = fx_read_shared(winlo, winhi, cc * g.wcells + t);
+            if (val == 0) continue;
+            if (!inside) {
+                atomicOr(a.status, ST_BOUNDS);
+                continue;
             }
+            if (FIXED) atomicAdd(a.fix[cc] + l, (unsigned long long)val);
+            else atomicAdd(a.cur[cc] + l, __double2float_rn(__ll2double_rn(val) * a.P.fx_inv));
         }
     }
 }
@@ -345,12 +424,11 @@ __global__ void __launch_bounds__(256, DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MI
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
     int *winhi = reinterpret_cast<int *>(smem_raw) + 3 * a.g.wcells;
-    float *winf = reinterpret_cast<float *>(smem_raw);
+
     const Geom &g = a.g;
     const int tile = blockIdx.x;
     const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
     WindowSink<FIXED> sink;
-    sink.s = winf;
     sink.lo = winlo;
     sink.hi = winhi;
     sink.wx0 = g.ox + tix * g.tx - g.wlo;
@@ -367,7 +445,7 @@ __global__ void __launch_bounds__(256, DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MI
     sink.scale = a.P.fx_scale;
     sink.g = &a.g;
     sink.status = a.status;
-    const int nwords = (FIXED ? 6 : 3) * g.wcells;
+    const int nwords = 6 * g.wcells;
     if (DEPOSIT) {
         for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
         __syncthreads();
