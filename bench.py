@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--sort-every", type=int, default=1)
+    ap.add_argument("--sort-every", type=int, default=0, help="0: chosen by the autotuner")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -233,14 +234,22 @@ def main():
     ws, rank, local = dist_setup(args)
     pkg = __graft_entry__.load_package()
     from tristan_gb300 import setups
-    cfg = setups.make_config(args.workload, diag_every=1, sort_every=args.sort_every)
+    cfg = setups.make_config(args.workload, diag_every=1, sort_every=max(args.sort_every, 1))
     ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
     setups.with_capacity(cfg, len(ions), len(lecs))
     n_p = len(ions) + len(lecs)
+    tuned = None
+    if args.impl == "gb300" and not args.no_autotune and args.sort_every == 0:
+        # tile shape and re-sort cadence for this plasma (before any timing)
+        from tristan_gb300.gpu import autotune
+        best, table = autotune(cfg, ions, lecs, laps=2, device=local)
+        tuned = {"tile": list(cfg.tile), "sort_every": cfg.sort_every, "best_ms_per_lap": best,
+                 "candidates": int(len(table))}
     grid = [cfg.nx, cfg.ny] + ([cfg.nz] if cfg.dims == 3 else [])
     config = {"workload": args.workload, "grid": grid, "order": cfg.order, "particles": n_p,
               "ppc_per_species": int(cfg.ppc0 // 2), "ntimes": cfg.ntimes, "deposit": "fp32-atomic",
               "diagnostics": "fp64 gauss/energy/momentum every lap", "sort_every": cfg.sort_every,
+              "tile": list(cfg.tile), "autotuned": tuned,
               "l2": "inputs larger than L2 (particle arrays %.1f GB), no flush" % (n_p * 44 / 1e9)}
 
     if args.impl == "reference":

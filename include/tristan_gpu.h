@@ -161,6 +161,17 @@ int tg_step(tg_ctx *ctx, int32_t nsteps);
 /* tg_step bracketed by CUDA events on the context's stream; *ms receives
    the device time of the nsteps laps. Synchronises. */
 int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms);
+/* Autotuner (no counterpart in the reference, which has no tunables of
+   this kind): times `laps` sort cycles of the fused lap for each candidate
+   tile shape (particles per tile follow from it) and re-sort cadence on the
+   caller's particles (p, ions, lecs as for tg_bind_particles, not
+   modified), and writes the fastest tile[] and sort_every into *cfg. If
+   table is non-NULL it receives up to table_len rows of (tx, ty, tz,
+   sort_every, ms per lap; -1 when the candidate failed). Returns the
+   number of rows, or a negative TG_ERR code when no candidate ran. */
+int tg_autotune(tg_config *cfg, void *p, int32_t ions, int32_t lecs, int32_t laps, float *best_ms,
+                float *table, int32_t table_len);
+
 /* FP64 Gauss-law residual, energies and momenta of the device state.
    Synchronises. */
 int tg_diag_fp64(tg_ctx *ctx, tg_diag *out);

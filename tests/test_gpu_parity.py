@@ -268,3 +268,18 @@ def test_small_tiles_force_global_fallback():
     g.sync_to_host()
     assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz"))
     g.close()
+
+
+def test_autotune_picks_a_runnable_layout_that_stays_exact():
+    from tristan_gb300.gpu import autotune
+    cfg = small_cfg(2, 3, fixed=1)
+    ions, lecs = beams(cfg)
+    best, table = autotune(cfg, ions, lecs, laps=1)
+    assert best > 0 and len(table) >= 3
+    assert cfg.sort_every in (1, 2, 3) and cfg.tile[0] > 0
+    o, g = pair(cfg, ions, lecs)
+    g.step(7)
+    o.step(7)
+    g.sync_to_host()
+    assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz"))
+    g.close()

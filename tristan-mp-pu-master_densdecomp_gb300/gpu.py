@@ -78,7 +78,7 @@ ENTRY_POINTS = (
     "tg_advance_e", "tg_move", "tg_reset_currents", "tg_deposit", "tg_fold_currents",
     "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_diag_fp64", "tg_synchronize",
     "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step", "tg_diag_history",
-    "tg_enable_timing", "tg_phase_times", "tg_step_timed", "tg_filter_noalloc",
+    "tg_enable_timing", "tg_phase_times", "tg_step_timed", "tg_filter_noalloc", "tg_autotune",
 )
 PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
@@ -127,6 +127,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_diag_history.restype = ctypes.c_int
     lib.tg_step_timed.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]
     lib.tg_step_timed.restype = ctypes.c_int
+    lib.tg_autotune.argtypes = [ctypes.POINTER(tg_config), P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                ctypes.POINTER(ctypes.c_float), P, ctypes.c_int32]
+    lib.tg_autotune.restype = ctypes.c_int
     lib.tg_enable_timing.argtypes = [P, ctypes.c_int32]
     lib.tg_enable_timing.restype = ctypes.c_int
     lib.tg_phase_times.argtypes = [P, ctypes.c_void_p, ctypes.c_int32]
@@ -159,6 +162,28 @@ def make_tg_config(cfg: SimConfig, device: int = 0) -> tg_config:
     c.device = device
     c.diag_every = int(cfg.diag_every)
     return c
+
+
+def autotune(cfg: SimConfig, ions: np.ndarray, lecs: np.ndarray, laps: int = 2, device: int = 0):
+    """Pick tile shape and re-sort cadence for this domain and plasma
+    (tg_autotune); updates cfg.tile / cfg.sort_every in place and returns
+    (best ms per lap, table of (tx, ty, tz, sort_every, ms))."""
+    lib = load_library()
+    if cfg.maxhlf == 0:
+        cfg.maxhlf = int(max(len(ions), len(lecs)) * 1.25) + 1024
+    p = np.zeros(2 * cfg.maxhlf, PARTICLE_DTYPE)
+    p[: len(ions)] = ions
+    p[cfg.maxhlf: cfg.maxhlf + len(lecs)] = lecs
+    c = make_tg_config(cfg, device)
+    best = ctypes.c_float()
+    table = np.zeros((64, 5), np.float32)
+    rows = lib.tg_autotune(ctypes.byref(c), p.ctypes.data, len(ions), len(lecs), int(laps), ctypes.byref(best),
+                           table.ctypes.data, 64)
+    if rows < 0:
+        raise TristanGpuError(-rows, "autotune: no candidate ran")
+    cfg.tile = (int(c.tile[0]), int(c.tile[1]), int(c.tile[2]))
+    cfg.sort_every = int(c.sort_every)
+    return float(best.value), table[:rows]
 
 
 _cudart = None
