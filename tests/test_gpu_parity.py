@@ -283,3 +283,60 @@ def test_autotune_picks_a_runnable_layout_that_stays_exact():
     g.sync_to_host()
     assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz"))
     g.close()
+
+
+@pytest.mark.parametrize("dims,order", [(2, 1), (2, 3), (3, 2)])
+def test_open_x_boundary_discards_like_the_reference(dims, order):
+    """x open (periodicx = 0): particles leaving [x1in, x2in] are discarded
+    (deposit_particles' boundary loop); counts, survivors and fields match"""
+    cfg = small_cfg(dims, order, fixed=1, periodic=(0, 1, 1))
+    ions, lecs = beams(cfg)
+    o, g = pair(cfg, ions, lecs)
+    g.step(5)
+    o.step(5)
+    g.sync_to_host()
+    ni, nl = g.counts()
+    assert (ni, nl) == (o.st.ions, o.st.lecs)
+    assert ni < len(ions)  # some left through the open faces
+    assert_particles_equal(g.ions, o.ions)
+    assert_particles_equal(g.lecs, o.lecs)
+    assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz"))
+    g.close()
+
+
+def test_external_constant_field_in_mover():
+    """get_external_fields hook: a constant external B in the mover"""
+    cfg = small_cfg(2, 2, fixed=1, external_fields=1, ext=(0.0, 0.0, 0.0, 0.0, 0.0, 0.05))
+    ions, lecs = beams(cfg)
+    o, g = pair(cfg, ions, lecs)
+    g.step(3)
+    o.step(3)
+    g.sync_to_host()
+    assert_particles_equal(g.ions, o.ions)
+    assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz"))
+    g.close()
+
+
+def test_failure_detection_overflow_and_out_of_grid():
+    """errors come back as status codes, never as a GPU fault: a species
+    count above maxhlf is refused on upload, and a particle outside the grid
+    is flagged by the device status word and dropped"""
+    from tristan_gb300.gpu import TG_ERR_BOUNDS, TG_ERR_OVERFLOW, TristanGpuError
+    cfg = small_cfg(2, 1, maxhlf=64)
+    ions, lecs = setups.load_beams(cfg, seed=3)
+    g = gpu_sim(cfg)
+    with pytest.raises(TristanGpuError) as e:
+        g._ions.value = cfg.maxhlf + 1
+        g.sync_from_host(8)
+    assert e.value.code == TG_ERR_OVERFLOW
+    bad = ions[:8].copy()
+    bad["x"][3] = -50.0  # outside the array
+    g.set_particles(bad, lecs[:8], upload=False)
+    g._ions.value, g._lecs.value = 8, 8
+    g.sync_from_host(8)
+    with pytest.raises(TristanGpuError) as e:
+        g.synchronize()
+    assert e.value.code == TG_ERR_BOUNDS
+    g.synchronize()  # the status word was cleared with the report
+    assert g.counts() == (7, 8)
+    g.close()

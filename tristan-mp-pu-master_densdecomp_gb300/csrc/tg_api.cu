@@ -442,6 +442,7 @@ extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
         }
         CK(cudaStreamSynchronize(ctx->st));  // n[] lives on this stack frame
         ctx->dirty = true;
+        ctx->may_have_dead = true;  // records outside the grid were dropped
     }
     return TG_OK;
 }
