@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--sort-every", type=int, default=0, help="0: chosen by the autotuner")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ens-boxes", type=int, default=64)
+    ap.add_argument("--ens-steps", type=int, default=40)
     return ap.parse_args()
 
 
@@ -229,6 +232,86 @@ def cpu_baseline(cfg, ions, lecs, steps):
     return dt, sim.lib.to_num_threads()
 
 
+def run_ensemble(args, device):
+    """The 64-box ensemble: the batched fixed-point form (one launch per
+    phase for all boxes, graph-replayed) against the plain form (one
+    single-domain context per box, stepped box after box), both on the same
+    seeded boxes, tile shape and sort cadence; no diagnostics in the timed
+    laps of either. Particle-steps/s are aggregated over all boxes."""
+    from tristan_gb300 import setups
+    from tristan_gb300.gpu import EnsembleSim, GpuSim, ensemble_autotune
+    t0 = time.perf_counter()
+    cfgs, table = setups.ensemble_configs(nbox=args.ens_boxes, seed=20240607)
+    parts = setups.load_ensemble(cfgs)
+    t_load = time.perf_counter() - t0
+    counts = [len(i) + len(l) for i, l in parts]
+    n_p = sum(counts)
+    # autotune on a sample of boxes: the two largest of each shape order
+    sample = []
+    for o in (1, 2, 3):
+        idx = sorted((b for b, c in enumerate(cfgs) if c.order == o), key=lambda b: -counts[b])[:2]
+        sample += idx
+    tuned = None
+    if not args.no_autotune and sample:
+        scfg = [cfgs[b] for b in sample]
+        best, tab = ensemble_autotune(scfg, [parts[b] for b in sample], laps=1, device=device)
+        for c in cfgs:
+            c.tile, c.sort_every = scfg[0].tile, scfg[0].sort_every
+        tuned = {"tile": list(scfg[0].tile), "sort_every": scfg[0].sort_every, "sample_boxes": sample,
+                 "best_ms_per_lap_on_sample": best, "candidates": int(len(tab))}
+    se = cfgs[0].sort_every
+    warm = max(args.warmup, 2 * se)
+    K = max(2 * se, args.ens_steps // (2 * se) * (2 * se))
+
+    def batched(fixed):
+        for c in cfgs:
+            c.fixed = int(fixed)
+        e = EnsembleSim(cfgs, device=device)
+        for b, (ions, lecs) in enumerate(parts):
+            e.set_particles(b, ions, lecs)
+        e.sync_from_host()
+        e.step(warm)
+        e.synchronize()
+        ms = e.step_timed(K)
+        res = max(e.diagnostics(b)["gauss_residual"] for b in range(e.nbox))
+        kps = e.kernels_per_step()
+        e.close()
+        return ms, res, kps
+
+    def plain(fixed):
+        total = 0.0
+        for b, c in enumerate(cfgs):
+            c.fixed = int(fixed)
+            g = GpuSim(c, device=device)
+            g.set_particles(*parts[b])
+            g.step(warm)
+            g.synchronize()
+            total += g.step_timed(K)
+            g.close()
+        return total
+
+    ms_bf, res_bf, kps = batched(True)
+    ms_b32, res_b32, _ = batched(False)
+    ms_pf = plain(True)
+    ms_p32 = plain(False)
+    rate = lambda ms: n_p * K / (ms / 1e3)
+    orders = {o: sum(1 for c in cfgs if c.order == o) for o in (1, 2, 3)}
+    return {
+        "workload": "ensemble of %d periodic 2D boxes (seeded sides, plasmas, shape orders)" % len(cfgs),
+        "boxes": len(cfgs), "particles": n_p, "cells": int(sum(c.nx * c.ny for c in cfgs)),
+        "boxes_per_order": orders, "seed": 20240607, "steps": K, "warmup": warm,
+        "tile": list(cfgs[0].tile), "sort_every": se, "autotuned": tuned,
+        "batched_fixed": {"value": rate(ms_bf), "ms_per_step": ms_bf / K, "gauss_residual_max": res_bf},
+        "batched_fp32": {"value": rate(ms_b32), "ms_per_step": ms_b32 / K, "gauss_residual_max": res_b32},
+        "plain_fp32": {"value": rate(ms_p32), "ms_per_step": ms_p32 / K,
+                       "form": "one single-domain context per box, boxes stepped one after another"},
+        "plain_fixed": {"value": rate(ms_pf), "ms_per_step": ms_pf / K},
+        "batched_fixed_over_plain_fp32": ms_p32 / ms_bf,
+        "batched_fixed_over_plain_fixed": ms_pf / ms_bf,
+        "kernels_per_step": kps, "host_load_s": t_load,
+    }
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup(args)
@@ -306,6 +389,9 @@ def main():
         cpu = {"value": n_p * args.cpu_steps / dt_cpu, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_steps} full laps of the workload (after 1 warm-up lap) on the OpenMP "
                          "CPU restatement; the Fortran reference cannot be built on the box"}
+    ens = None
+    if rank == 0 and not args.no_ensemble:
+        ens = run_ensemble(args, device)
     if rank != 0:
         return
     d = hist[-1] if len(hist) else None
@@ -314,7 +400,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config, "fixed_point": fixed, "phase_ms_per_lap": phases,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": kps * args.steps,
+            "gpu_launches": kps * args.steps, "ensemble": ens,
             "gauss_residual_last_lap": (float(np.sqrt(d[0] / d[1])) if d is not None and d[1] > 0 else None)}
     print(json.dumps(line), flush=True)
 

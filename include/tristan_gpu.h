@@ -221,6 +221,47 @@ void *tg_stream(tg_ctx *ctx);
 /* Number of kernels launched by the last tg_step lap (for accounting). */
 int32_t tg_kernels_per_step(tg_ctx *ctx);
 
+/* ---------------------------------------------------------------------
+   Batched ensemble: many independent periodic 2D boxes of uneven size
+   (seed or parameter ensembles) stepped together, one launch per phase for
+   all boxes, the laps replayed from a captured CUDA graph. No counterpart
+   in the reference, which runs one domain per job; each box is what one
+   run of its main loop steps (code/tristanmainloop.F90:117-303), and the
+   per-box entry points mirror the single-domain ones above (same
+   arguments with a box index, same error codes). All boxes share the
+   deposit mode, the sort cadence, ntimes and the device; boxes may differ
+   in size, shape order, plasma and charges. In fixed-point mode every box
+   evolves bit for bit as a single-domain context of the same
+   configuration. Not thread-safe per ensemble.
+   --------------------------------------------------------------------- */
+typedef struct tg_ens tg_ens;
+/* cfgs[0..nbox): one tg_config per box (dims 2, periodic x and y). */
+int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out);
+void tg_ens_finalize(tg_ens *ens);
+/* Message of the last failure (ens NULL: of the last failed tg_ens_init). */
+const char *tg_ens_last_error(tg_ens *ens);
+int tg_ens_bind_fields(tg_ens *ens, int32_t box, float *ex, float *ey, float *ez, float *bx, float *by, float *bz,
+                       float *curx, float *cury, float *curz);
+int tg_ens_bind_particles(tg_ens *ens, int32_t box, void *p, int32_t *ions, int32_t *lecs);
+/* Copies of the bound host arrays of every box, as tg_sync_from_host /
+   tg_sync_to_host. */
+int tg_ens_sync_from_host(tg_ens *ens, unsigned mask);
+int tg_ens_sync_to_host(tg_ens *ens, unsigned mask);
+/* nsteps laps of every box. */
+int tg_ens_step(tg_ens *ens, int32_t nsteps);
+int tg_ens_step_timed(tg_ens *ens, int32_t nsteps, float *ms);
+/* FP64 diagnostics of one box (as tg_diag_fp64). Synchronises. */
+int tg_ens_diag_fp64(tg_ens *ens, int32_t box, tg_diag *out);
+int tg_ens_get_counts(tg_ens *ens, int32_t box, int64_t *ions, int64_t *lecs);
+int tg_ens_synchronize(tg_ens *ens);
+int32_t tg_ens_kernels_per_step(tg_ens *ens);
+/* Autotuner of the ensemble: one tile shape and sort cadence for all boxes,
+   timed on the given boxes (p[b], *ions[b], *lecs[b] as for
+   tg_ens_bind_particles, not modified); writes tile[] and sort_every into
+   every cfgs[b]. table rows and return value as tg_autotune. */
+int tg_ens_autotune(tg_config *cfgs, int32_t nbox, void *const *p, int32_t *const *ions, int32_t *const *lecs,
+                    int32_t laps, float *best_ms, float *table, int32_t table_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -113,18 +113,25 @@ static int check_status(tg_ctx *ctx) {
 // ---------------------------------------------------------------------------
 // geometry
 // ---------------------------------------------------------------------------
-static int setup_geom(tg_ctx *ctx) {
-    const tg_config &c = ctx->cfg;
-    Geom &g = ctx->g;
+// failures write their message to err[0..errlen)
+static int geom_fail(char *err, size_t errlen, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(err, errlen, fmt, ap);
+    va_end(ap);
+    return TG_ERR_ARG;
+}
+
+int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     memset(&g, 0, sizeof g);
-    if (c.dims != 2 && c.dims != 3) return fail(ctx, TG_ERR_ARG, "dims must be 2 or 3 (got %d)", c.dims);
-    if (c.order < 1 || c.order > 3) return fail(ctx, TG_ERR_ARG, "order must be 1, 2 or 3 (got %d)", c.order);
+    if (c.dims != 2 && c.dims != 3) return geom_fail(err, errlen, "dims must be 2 or 3 (got %d)", c.dims);
+    if (c.order < 1 || c.order > 3) return geom_fail(err, errlen, "order must be 1, 2 or 3 (got %d)", c.order);
     const int ng_expect = c.order == 1 ? 5 : 7;
     if (c.nghost != ng_expect)
-        return fail(ctx, TG_ERR_ARG, "nghost must be %d for order %d (got %d)", ng_expect, c.order, c.nghost);
+        return geom_fail(err, errlen, "nghost must be %d for order %d (got %d)", ng_expect, c.order, c.nghost);
     if (c.dims == 2 && (c.mz != 1 || c.nghostz != 5))
-        return fail(ctx, TG_ERR_ARG, "2D needs mz = 1 and nghostz = 5");
-    if (c.dims == 3 && c.nghostz != c.nghost) return fail(ctx, TG_ERR_ARG, "3D needs nghostz = nghost");
+        return geom_fail(err, errlen, "2D needs mz = 1 and nghostz = 5");
+    if (c.dims == 3 && c.nghostz != c.nghost) return geom_fail(err, errlen, "3D needs nghostz = nghost");
     g.dims = c.dims;
     g.order = c.order;
     g.mx = c.mx;
@@ -134,9 +141,9 @@ static int setup_geom(tg_ctx *ctx) {
     g.ngz = c.nghostz;
     const int nx = c.mx - g.ng, ny = c.my - g.ng, nz = c.dims == 3 ? c.mz - g.ngz : 1;
     if (nx < 4 || ny < 4 || nz < 1 || (c.dims == 3 && nz < 4))
-        return fail(ctx, TG_ERR_ARG, "grid too small (%d x %d x %d interior cells)", nx, ny, nz);
+        return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells)", nx, ny, nz);
     g.lot = (long long)c.mx * c.my * c.mz;
-    if (g.lot >= (1LL << 31)) return fail(ctx, TG_ERR_ARG, "grid of %lld cells exceeds int32 cell indices", g.lot);
+    if (g.lot >= (1LL << 31)) return geom_fail(err, errlen, "grid of %lld cells exceeds int32 cell indices", g.lot);
     g.sy = c.mx;
     g.sz = (long long)c.mx * c.my;
     for (int a = 0; a < 3; a++) g.per[a] = c.periodic[a] ? 1 : 0;
@@ -178,13 +185,11 @@ static int setup_geom(tg_ctx *ctx) {
     g.wcells = g.wx * g.wy * g.wz;
     const size_t smem = (size_t)6 * g.wcells * 4;  // split 32-bit window, 3 components
     if (smem > 227 * 1024)
-        return fail(ctx, TG_ERR_ARG, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
+        return geom_fail(err, errlen, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
     return TG_OK;
 }
 
-static void setup_params(tg_ctx *ctx) {
-    const tg_config &c = ctx->cfg;
-    Params &P = ctx->P;
+void tg::build_params(const tg_config &c, Params &P) {
     memset(&P, 0, sizeof P);
     P.c = c.c;
     P.corr = c.corr;
@@ -201,6 +206,10 @@ static void setup_params(tg_ctx *ctx) {
     P.fx_inv = ldexp(1.0, -c.fx_shift);
     P.quirks = c.quirks;
 }
+
+static int setup_geom(tg_ctx *ctx) { return build_geom(ctx->cfg, ctx->g, ctx->err, sizeof ctx->err); }
+
+static void setup_params(tg_ctx *ctx) { build_params(ctx->cfg, ctx->P); }
 
 static int alloc_species(tg_ctx *ctx, Species &s, size_t n) {
     int r;
@@ -665,7 +674,7 @@ static int run_diag(tg_ctx *ctx, bool particles) {
     return TG_OK;
 }
 
-static void record_to_diag(const double *h, tg_diag *out) {
+void tg::record_to_diag(const double *h, tg_diag *out) {
     memset(out, 0, sizeof *out);
     out->gauss_abs = sqrt(h[0]);
     out->rho_norm = sqrt(h[1]);

@@ -395,6 +395,13 @@ cudaError_t launch_soa_to_aos(const Geom &g, const Species &sp, void *out, long 
 // error text readable through tg_last_error(NULL) (tg_api.cu)
 void tg_set_global_error(const char *msg);
 
+// geometry and constants of one domain from its configuration (tg_api.cu);
+// build_geom returns TG_OK or TG_ERR_ARG with the reason in err
+int build_geom(const tg_config &c, Geom &g, char *err, size_t errlen);
+void build_params(const tg_config &c, Params &P);
+// one diagnostics record (16 doubles) as a tg_diag
+void record_to_diag(const double *h, tg_diag *out);
+
 // FP64 diagnostics (tg_diag.cu)
 struct DiagLaunch {
     Geom g;

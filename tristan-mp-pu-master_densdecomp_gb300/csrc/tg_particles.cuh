@@ -256,61 +256,70 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
         const int loz = min(b1z, b2z);
         const int nz = max(b1z, b2z) + NS - loz;
         const int kbase = k1 - 3 + loz;
-        // x-y weights of the z current, one per (x,y) slot
-        float wxy[U][U];
-#pragma unroll
-        for (int rx = 0; rx < U; rx++) {
-#pragma unroll
-            for (int ry = 0; ry < U; ry++) {
-                const float dSx = S2x[rx] - S1x[rx], dSy = S2y[ry] - S1y[ry];
-                wxy[rx][ry] = S1x[rx] * S1y[ry] + TG_HALF * dSx * S1y[ry] + TG_HALF * S1x[rx] * dSy +
-                              TG_THIRD * dSx * dSy;
-            }
-        }
-        float czp[U][U];
-#pragma unroll
-        for (int rx = 0; rx < U; rx++)
-#pragma unroll
-            for (int ry = 0; ry < U; ry++) czp[rx][ry] = 0.0f;
         float S1z[U], S2z[U];
 #pragma unroll
         for (int r = 0; r < U; r++) {
             S1z[r] = pick<NS>(w1z, r, b1z - loz);
             S2z[r] = pick<NS>(w2z, r, b2z - loz);
         }
-        // planes rolled (code size), each plane's cells unrolled
+        // The three components' carries form independent chains: cx one
+        // chain over all cells in the reference's (z, y, x) order, cy one
+        // chain per x slot over (z, y), cz one chain per (x, y) slot over z.
+        // Each chain is walked in its own order below, so every cell gets
+        // exactly the reference's value while only one row of carries is
+        // live at a time (the window sums are order independent).
+        // cx and cy: planes and rows rolled, the row's cells unrolled
 #pragma unroll 1
         for (int rz = 0; rz < nz; rz++) {
-            {
-                const float s1z = sel<U>(S1z, rz);
-                const float dSz = sel<U>(S2z, rz) - s1z;
-                float wxz[U];
+            const float s1z = sel<U>(S1z, rz);
+            const float dSz = sel<U>(S2z, rz) - s1z;
+            float wxz[U];
+#pragma unroll
+            for (int rx = 0; rx < U; rx++) {
+                const float dSx = S2x[rx] - S1x[rx];
+                wxz[rx] = S1x[rx] * s1z + TG_HALF * dSx * s1z + TG_HALF * S1x[rx] * dSz + TG_THIRD * dSx * dSz;
+            }
+#pragma unroll 1
+            for (int ry = 0; ry < ny; ry++) {
+                const float s1y = sel<U>(S1y, ry);
+                const float dSy = sel<U>(S2y, ry) - s1y;
+                const float wyz = s1y * s1z + TG_HALF * dSy * s1z + TG_HALF * s1y * dSz + TG_THIRD * dSy * dSz;
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
-                    const float dSx = S2x[rx] - S1x[rx];
-                    wxz[rx] = S1x[rx] * s1z + TG_HALF * dSx * s1z + TG_HALF * S1x[rx] * dSz + TG_THIRD * dSx * dSz;
+                    if (rx < nx) {
+                        const float dSx = S2x[rx] - S1x[rx];
+                        const float cx = q * (dSx * wyz) + cxp;
+                        const float cy = q * (dSy * wxz[rx]) + cyp[rx];
+                        sink.add(0, ibase + rx, jbase + ry, kbase + rz, cx);
+                        sink.add(1, ibase + rx, jbase + ry, kbase + rz, cy);
+                        cxp = cx;
+                        cyp[rx] = cy;
+                    }
                 }
+            }
+        }
+        // cz: rows rolled, planes rolled inside, the row's cells unrolled
+#pragma unroll 1
+        for (int ry = 0; ry < ny; ry++) {
+            const float s1y = sel<U>(S1y, ry);
+            const float dSy = sel<U>(S2y, ry) - s1y;
+            float wxy[U], czp[U];
 #pragma unroll
-                for (int ry = 0; ry < U; ry++) {
-                    if (ry < ny) {
-                        const float dSy = S2y[ry] - S1y[ry];
-                        const float wyz = S1y[ry] * s1z + TG_HALF * dSy * s1z + TG_HALF * S1y[ry] * dSz +
-                                          TG_THIRD * dSy * dSz;
+            for (int rx = 0; rx < U; rx++) {
+                const float dSx = S2x[rx] - S1x[rx];
+                wxy[rx] = S1x[rx] * s1y + TG_HALF * dSx * s1y + TG_HALF * S1x[rx] * dSy + TG_THIRD * dSx * dSy;
+                czp[rx] = 0.0f;
+            }
+#pragma unroll 1
+            for (int rz = 0; rz < nz; rz++) {
+                const float s1z = sel<U>(S1z, rz);
+                const float dSz = sel<U>(S2z, rz) - s1z;
 #pragma unroll
-                        for (int rx = 0; rx < U; rx++) {
-                            if (rx < nx) {
-                                const float dSx = S2x[rx] - S1x[rx];
-                                const float cx = q * (dSx * wyz) + cxp;
-                                const float cy = q * (dSy * wxz[rx]) + cyp[rx];
-                                const float cz = q * (dSz * wxy[rx][ry]) + czp[rx][ry];
-                                sink.add(0, ibase + rx, jbase + ry, kbase + rz, cx);
-                                sink.add(1, ibase + rx, jbase + ry, kbase + rz, cy);
-                                sink.add(2, ibase + rx, jbase + ry, kbase + rz, cz);
-                                cxp = cx;
-                                cyp[rx] = cy;
-                                czp[rx][ry] = cz;
-                            }
-                        }
+                for (int rx = 0; rx < U; rx++) {
+                    if (rx < nx) {
+                        const float cz = q * (dSz * wxy[rx]) + czp[rx];
+                        sink.add(2, ibase + rx, jbase + ry, kbase + rz, cz);
+                        czp[rx] = cz;
                     }
                 }
             }
@@ -419,14 +428,21 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
 #ifndef TG_TILES_MINB_3D
 #define TG_TILES_MINB_3D 2
 #endif
+// threads per tile CTA: 3D tiles hold more particles and a larger window,
+// so two CTAs of 512 threads share an SM's shared memory
+#ifndef TG_TILE_THREADS_3D
+#define TG_TILE_THREADS_3D 256
+#endif
+#define TG_TILE_THREADS(DIM) ((DIM) == 3 ? TG_TILE_THREADS_3D : 256)
+// One tile: push, deposit into the shared window, wrap, flush. Every thread
+// of the CTA calls it with the same tile (it contains barriers); smem_raw is
+// the 6 * wcells words of the window.
 template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
-__global__ void __launch_bounds__(256, DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MINB_2D) k_tiles(TileArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, unsigned char *smem_raw) {
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
     int *winhi = reinterpret_cast<int *>(smem_raw) + 3 * a.g.wcells;
 
     const Geom &g = a.g;
-    const int tile = blockIdx.x;
     const int tix = tile % g.ntx, tiy = (tile / g.ntx) % g.nty, tiz = tile / (g.ntx * g.nty);
     WindowSink<FIXED> sink;
     sink.lo = winlo;
@@ -524,6 +540,13 @@ __global__ void __launch_bounds__(256, DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MI
     }
 }
 
+template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
+__global__ void __launch_bounds__(TG_TILE_THREADS(DIM), DIM == 3 ? TG_TILES_MINB_3D : TG_TILES_MINB_2D)
+    k_tiles(TileArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_body<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, blockIdx.x, smem_raw);
+}
+
 // ---------------------------------------------------------------------------
 // mover alone over [0, count)
 // ---------------------------------------------------------------------------
@@ -562,7 +585,7 @@ namespace tg {
 template <int DIM, int ORDER>
 cudaError_t launch_tiles_o(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st,
                                   size_t smem) {
-    dim3 grid(a.g.ntiles), block(256);
+    dim3 grid(a.g.ntiles), block(TG_TILE_THREADS(DIM));
 #define TG_L(F, PU, DE)                                                                              \
     do {                                                                                             \
         auto kern = k_tiles<DIM, ORDER, F, PU, DE>;                                                  \

@@ -79,6 +79,9 @@ ENTRY_POINTS = (
     "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_diag_fp64", "tg_synchronize",
     "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step", "tg_diag_history",
     "tg_enable_timing", "tg_phase_times", "tg_step_timed", "tg_filter_noalloc", "tg_autotune",
+    "tg_ens_init", "tg_ens_finalize", "tg_ens_last_error", "tg_ens_bind_fields", "tg_ens_bind_particles",
+    "tg_ens_sync_from_host", "tg_ens_sync_to_host", "tg_ens_step", "tg_ens_step_timed", "tg_ens_diag_fp64",
+    "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
 )
 PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
@@ -134,6 +137,36 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_enable_timing.restype = ctypes.c_int
     lib.tg_phase_times.argtypes = [P, ctypes.c_void_p, ctypes.c_int32]
     lib.tg_phase_times.restype = ctypes.c_int
+    # batched ensemble
+    lib.tg_ens_init.argtypes = [ctypes.POINTER(tg_config), ctypes.c_int32, ctypes.POINTER(P)]
+    lib.tg_ens_init.restype = ctypes.c_int
+    lib.tg_ens_finalize.argtypes = [P]
+    lib.tg_ens_finalize.restype = None
+    lib.tg_ens_last_error.argtypes = [P]
+    lib.tg_ens_last_error.restype = ctypes.c_char_p
+    lib.tg_ens_bind_fields.argtypes = [P, ctypes.c_int32] + [P] * 9
+    lib.tg_ens_bind_fields.restype = ctypes.c_int
+    lib.tg_ens_bind_particles.argtypes = [P, ctypes.c_int32, P, P, P]
+    lib.tg_ens_bind_particles.restype = ctypes.c_int
+    for n in ("tg_ens_sync_from_host", "tg_ens_sync_to_host"):
+        getattr(lib, n).argtypes = [P, ctypes.c_uint]
+        getattr(lib, n).restype = ctypes.c_int
+    lib.tg_ens_step.argtypes = [P, ctypes.c_int32]
+    lib.tg_ens_step.restype = ctypes.c_int
+    lib.tg_ens_step_timed.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]
+    lib.tg_ens_step_timed.restype = ctypes.c_int
+    lib.tg_ens_diag_fp64.argtypes = [P, ctypes.c_int32, ctypes.POINTER(tg_diag)]
+    lib.tg_ens_diag_fp64.restype = ctypes.c_int
+    lib.tg_ens_get_counts.argtypes = [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_int64)]
+    lib.tg_ens_get_counts.restype = ctypes.c_int
+    lib.tg_ens_synchronize.argtypes = [P]
+    lib.tg_ens_synchronize.restype = ctypes.c_int
+    lib.tg_ens_kernels_per_step.argtypes = [P]
+    lib.tg_ens_kernels_per_step.restype = ctypes.c_int32
+    lib.tg_ens_autotune.argtypes = [ctypes.POINTER(tg_config), ctypes.c_int32, P, P, P, ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_float), P, ctypes.c_int32]
+    lib.tg_ens_autotune.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -364,10 +397,7 @@ class GpuSim:
     def diagnostics(self) -> dict:
         d = tg_diag()
         self._check(self.lib.tg_diag_fp64(self.h, ctypes.byref(d)))
-        out = {k: getattr(d, k) for k, _ in tg_diag._fields_}
-        out["p_part"] = list(d.p_part)
-        out["p_field"] = list(d.p_field)
-        return out
+        return _diag_dict(d)
 
     DIAG_KEYS = ("res2", "rho2", "charge_total", "e_field", "e_mag", "e_kin_ions", "e_kin_lecs",
                  "px", "py", "pz", "fx", "fy", "fz")
@@ -390,3 +420,164 @@ class GpuSim:
     def field(self, name: str) -> np.ndarray:
         c = self.cfg
         return self.fields[name].reshape(c.mz, c.my, c.mx)
+
+
+def _diag_dict(d: tg_diag) -> dict:
+    out = {k: getattr(d, k) for k, _ in tg_diag._fields_}
+    out["p_part"] = list(d.p_part)
+    out["p_field"] = list(d.p_field)
+    return out
+
+
+class EnsembleSim:
+    """Many independent periodic 2D boxes stepped together (tg_ens_*): one
+    launch per phase for all boxes. Each box keeps its own host arrays, laid
+    out as for GpuSim; ``pinned`` page-locks them."""
+
+    def __init__(self, cfgs, device: int = 0, pinned: bool = False):
+        self.cfgs = list(cfgs)
+        self.lib = load_library()
+        n = len(self.cfgs)
+        self.tcfgs = (tg_config * n)(*[make_tg_config(c, device) for c in self.cfgs])
+        h = ctypes.c_void_p()
+        rc = self.lib.tg_ens_init(self.tcfgs, n, ctypes.byref(h))
+        if rc != TG_OK:
+            raise TristanGpuError(rc, self.lib.tg_ens_last_error(None).decode())
+        self.h = h
+        self.fields, self.p, self._ions, self._lecs, self._pinned = [], [], [], [], []
+        for b, c in enumerate(self.cfgs):
+            lot = c.mx * c.my * c.mz
+            self.fields.append({k: np.zeros(lot, np.float32) for k in FIELD_NAMES})
+            self.p.append(np.zeros(2 * c.maxhlf, PARTICLE_DTYPE))
+            self._ions.append(ctypes.c_int32(0))
+            self._lecs.append(ctypes.c_int32(0))
+            if pinned:
+                rt = _cudart_lib()
+                for arr in [self.p[b]] + [self.fields[b][k] for k in FIELD_NAMES]:
+                    if rt.cudaHostRegister(arr.ctypes.data, arr.nbytes, 0) != 0:
+                        raise TristanGpuError(TG_ERR_CUDA, "cudaHostRegister failed")
+                    self._pinned.append(arr)
+            self._check(self.lib.tg_ens_bind_fields(self.h, b, *[self.fields[b][k].ctypes.data
+                                                                 for k in FIELD_NAMES]))
+            self._check(self.lib.tg_ens_bind_particles(self.h, b, self.p[b].ctypes.data,
+                                                       ctypes.addressof(self._ions[b]),
+                                                       ctypes.addressof(self._lecs[b])))
+
+    @property
+    def nbox(self) -> int:
+        return len(self.cfgs)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tg_ens_finalize(self.h)
+            self.h = None
+            for arr in getattr(self, "_pinned", []):
+                _cudart_lib().cudaHostUnregister(arr.ctypes.data)
+            self._pinned = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != TG_OK:
+            raise TristanGpuError(rc, self.lib.tg_ens_last_error(self.h).decode())
+
+    def set_particles(self, box: int, ions: np.ndarray, lecs: np.ndarray) -> None:
+        mh = self.cfgs[box].maxhlf
+        if len(ions) > mh or len(lecs) > mh:
+            raise TristanGpuError(TG_ERR_OVERFLOW, "particle count exceeds maxhlf")
+        self.p[box][: len(ions)] = ions
+        self.p[box][mh: mh + len(lecs)] = lecs
+        self._ions[box].value, self._lecs[box].value = len(ions), len(lecs)
+
+    def set_fields(self, box: int, **arrays) -> None:
+        for k, v in arrays.items():
+            self.fields[box][k][:] = np.asarray(v, np.float32).ravel()
+
+    def sync_from_host(self, mask: int = SYNC_ALL) -> None:
+        self._check(self.lib.tg_ens_sync_from_host(self.h, mask))
+
+    def sync_to_host(self, mask: int = SYNC_ALL) -> None:
+        self._check(self.lib.tg_ens_sync_to_host(self.h, mask))
+
+    def host_bytes(self, mask: int) -> int:
+        n = 0
+        for b, c in enumerate(self.cfgs):
+            per = c.mx * c.my * c.mz * 4
+            n += per * 3 * sum(1 for m in (SYNC_E, SYNC_B, SYNC_CUR) if mask & m)
+            if mask & SYNC_PARTICLES:
+                n += (self._ions[b].value + self._lecs[b].value) * PARTICLE_DTYPE.itemsize
+        return n
+
+    def ions(self, box: int) -> np.ndarray:
+        return self.p[box][: self._ions[box].value]
+
+    def lecs(self, box: int) -> np.ndarray:
+        mh = self.cfgs[box].maxhlf
+        return self.p[box][mh: mh + self._lecs[box].value]
+
+    def field(self, box: int, name: str) -> np.ndarray:
+        c = self.cfgs[box]
+        return self.fields[box][name].reshape(c.mz, c.my, c.mx)
+
+    def counts(self, box: int):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.tg_ens_get_counts(self.h, box, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def step(self, n: int = 1):
+        self._check(self.lib.tg_ens_step(self.h, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        ms = ctypes.c_float()
+        self._check(self.lib.tg_ens_step_timed(self.h, int(n), ctypes.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self):
+        self._check(self.lib.tg_ens_synchronize(self.h))
+
+    def kernels_per_step(self) -> int:
+        return int(self.lib.tg_ens_kernels_per_step(self.h))
+
+    def diagnostics(self, box: int) -> dict:
+        d = tg_diag()
+        self._check(self.lib.tg_ens_diag_fp64(self.h, box, ctypes.byref(d)))
+        return _diag_dict(d)
+
+
+def ensemble_autotune(cfgs, particles, laps: int = 2, device: int = 0):
+    """One tile shape and sort cadence for all boxes (tg_ens_autotune),
+    timed on `particles` = [(ions, lecs) per box]; updates every cfg in place
+    and returns (best ms per lap, table)."""
+    lib = load_library()
+    n = len(cfgs)
+    arrs, ni, nl = [], [], []
+    for c, (ions, lecs) in zip(cfgs, particles):
+        p = np.zeros(2 * c.maxhlf, PARTICLE_DTYPE)
+        p[: len(ions)] = ions
+        p[c.maxhlf: c.maxhlf + len(lecs)] = lecs
+        arrs.append(p)
+        ni.append(ctypes.c_int32(len(ions)))
+        nl.append(ctypes.c_int32(len(lecs)))
+    tc = (tg_config * n)(*[make_tg_config(c, device) for c in cfgs])
+    pp = (ctypes.c_void_p * n)(*[a.ctypes.data for a in arrs])
+    pi = (ctypes.c_void_p * n)(*[ctypes.addressof(x) for x in ni])
+    pl = (ctypes.c_void_p * n)(*[ctypes.addressof(x) for x in nl])
+    best = ctypes.c_float()
+    table = np.zeros((64, 5), np.float32)
+    rows = lib.tg_ens_autotune(tc, n, pp, pi, pl, int(laps), ctypes.byref(best), table.ctypes.data, 64)
+    if rows < 0:
+        raise TristanGpuError(-rows, "ensemble autotune: no candidate ran")
+    for c, t in zip(cfgs, tc):
+        c.tile = (int(t.tile[0]), int(t.tile[1]), int(t.tile[2]))
+        c.sort_every = int(t.sort_every)
+    return float(best.value), table[:rows]

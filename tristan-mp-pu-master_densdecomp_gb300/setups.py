@@ -22,7 +22,9 @@ shapes from numpy's PCG64 with a fixed seed:
 The named workloads follow the reference's benchmark configurations: a
 128x128 order-1 Weibel box (8 per cell per species), a 1024x1024 order-3
 two-stream/Weibel box (16 per cell per species, beams at +-0.5c), a 256^3
-order-2 Weibel box (4 per cell per species, gamma0 = 5).
+order-2 Weibel box (4 per cell per species, gamma0 = 5), and an ensemble of
+64 independent periodic 2D boxes whose sizes, plasmas and shape orders are
+drawn from one seeded generator (ensemble_configs).
 """
 from __future__ import annotations
 
@@ -118,3 +120,41 @@ def with_capacity(cfg: SimConfig, nions: int, nlecs: int) -> SimConfig:
     if cfg.maxhlf == 0:
         cfg.maxhlf = int(max(nions, nlecs) * 1.25) + 1024
     return cfg
+
+
+ENSEMBLE_SIDES = (128, 192, 256, 384, 512)
+
+
+def ensemble_configs(nbox: int = 64, seed: int = 20240607, sides=ENSEMBLE_SIDES, ppc_range=(4, 32),
+                     fixed: bool = True, **overrides):
+    """Per-box configurations of a seeded ensemble of periodic 2D boxes:
+    each side uniform on `sides`, particles per cell per species uniform on
+    the even numbers of `ppc_range` (two equal beams), beam gamma0 uniform on
+    [1.5, 10], kT/mc^2 log-uniform on [1e-3, 1e-1], shape order uniform on
+    {1, 2, 3}; c = 0.45, c_omp = 10, ntimes = 4. Returns (configs, table),
+    the table listing the draws per box."""
+    rng = np.random.default_rng(seed)
+    cfgs, table = [], []
+    for b in range(nbox):
+        nx = int(rng.choice(sides))
+        ny = int(rng.choice(sides))
+        nps = 2 * int(rng.integers(ppc_range[0] // 2, ppc_range[1] // 2 + 1))
+        gamma0 = float(rng.uniform(1.5, 10.0))
+        delgam = float(10.0 ** rng.uniform(-3.0, -1.0))
+        order = int(rng.integers(1, 4))
+        kw = dict(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=float(2 * nps),
+                  gamma0=gamma0, delgam=delgam, ntimes=4, fixed=int(fixed))
+        kw.update(overrides)
+        cfgs.append(SimConfig(**kw))
+        table.append(dict(box=b, nx=nx, ny=ny, ppc_species=nps, gamma0=gamma0, delgam=delgam, order=order))
+    return cfgs, table
+
+
+def load_ensemble(cfgs, seed: int = 123457):
+    """Beams of every box (box b drawn with seed + b); sets each maxhlf."""
+    out = []
+    for b, cfg in enumerate(cfgs):
+        ions, lecs = load_beams(cfg, seed=seed + b)
+        with_capacity(cfg, len(ions), len(lecs))
+        out.append((ions, lecs))
+    return out
