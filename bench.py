@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--ens-boxes", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=40)
+    ap.add_argument("--ens-tile", type=int, nargs=2, default=None,
+                    help="tile shape of the ensemble (with --no-autotune)")
     return ap.parse_args()
 
 
@@ -259,6 +261,9 @@ def run_ensemble(args, device):
             c.tile, c.sort_every = scfg[0].tile, scfg[0].sort_every
         tuned = {"tile": list(scfg[0].tile), "sort_every": scfg[0].sort_every, "sample_boxes": sample,
                  "best_ms_per_lap_on_sample": best, "candidates": int(len(tab))}
+    elif args.ens_tile:
+        for c in cfgs:
+            c.tile, c.sort_every = (args.ens_tile[0], args.ens_tile[1], 1), max(args.sort_every, 1)
     se = cfgs[0].sort_every
     warm = max(args.warmup, 2 * se)
     K = max(2 * se, args.ens_steps // (2 * se) * (2 * se))
@@ -277,6 +282,11 @@ def run_ensemble(args, device):
         kps = e.kernels_per_step()
         e.close()
         return ms, res, kps
+
+    if args.workload == "ensemble64" and args.no_fixed:
+        # profiling: the batched fixed-point form alone
+        ms_bf, res_bf, kps = batched(True)
+        return {"batched_fixed": {"value": n_p * K / (ms_bf / 1e3), "ms_per_step": ms_bf / K}}
 
     def plain(fixed):
         total = 0.0
@@ -316,6 +326,13 @@ def main():
     args = parse()
     ws, rank, local = dist_setup(args)
     pkg = __graft_entry__.load_package()
+    if args.workload == "ensemble64":
+        # the ensemble alone (its numbers also ride on the default line)
+        if rank == 0:
+            ens = run_ensemble(args, local)
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "ensemble64", "ensemble": ens}),
+                  flush=True)
+        return
     from tristan_gb300 import setups
     cfg = setups.make_config(args.workload, diag_every=1, sort_every=max(args.sort_every, 1))
     ions, lecs = setups.load_beams(cfg, seed=123457 + rank)

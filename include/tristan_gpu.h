@@ -222,6 +222,56 @@ void *tg_stream(tg_ctx *ctx);
 int32_t tg_kernels_per_step(tg_ctx *ctx);
 
 /* ---------------------------------------------------------------------
+   Collisionless-shock hooks (2D): the user_* routines of
+   user_pu/user_shock_pu.F90 run as device kernels, so the main loop stays
+   on the GPU. Replaces particle_bc_user (:514-611, the left reflecting
+   wall with its zigzag partial deposits, code/particles.F90:550-669),
+   field_bc_user (:460-488, conductor behind the wall and upstream fields
+   at the right edge) and inject_particles_user (:364-395, the moving
+   injector with rightclean = 0 and rightwall = 0) with
+   inject_from_wall / inject_plasma_region (code/particles.F90:2439-2938)
+   and the Park-Miller generator and Maxwell-Juttner loader
+   (code/aux.F90:82-134, code/particles.F90:2126-2273). Random draws follow
+   the reference's sequence: pair k of an injection starts 13k draws (plus
+   any gamma redraws before it) after the call's first draw, so ind, counts
+   and positions are the reference's. With the hooks set, tg_step runs them
+   at their places in the lap and sorts every lap (sort_every must be 1).
+   --------------------------------------------------------------------- */
+typedef struct {
+    int32_t wall;                 /* left wall on */
+    double walloc;                /* wall position, global x */
+    float gammawall, betawall;    /* wallgam and its beta */
+    int32_t cond_i1, cond_i2;     /* ey = ez = 0 on local i in [cond_i1, cond_i2] (if different) */
+    int32_t edge_i1, edge_i2;     /* upstream fields on i in [edge_i1, edge_i2] (if different) */
+    float edge[6];                /* ex ey ez bx by bz written there */
+    int32_t inject;               /* moving injector on */
+    double xinject2;              /* injector position, global x */
+    float betainj;                /* injector speed / c */
+    double xinj_max;              /* mx0 - 15: the injector stops there */
+    float ppc0, gamma_drift, weight;
+    float y1, y2;                 /* injection band, global y */
+    float delgam_i, delgam_e;     /* kT / m c^2 of ions and electrons */
+    float pcosthmult;             /* 1: 3D Maxwellians (table and angles) */
+    int32_t sigma_nonzero;        /* magnetised: one more pcosth draw */
+    double dseed;                 /* generator state (an integer in a double) */
+    int32_t totalpartnum;         /* last ind handed out */
+} tg_shock;
+/* Set (or replace) the hooks; builds the Maxwell-Juttner tables on the
+   host. Errors: TG_ERR_ARG (3D domain, sort_every != 1). */
+int tg_shock_init(tg_ctx *ctx, const tg_shock *shock);
+/* Current injector / wall / generator state (synchronises). */
+int tg_shock_get(tg_ctx *ctx, tg_shock *out);
+/* inject_plasma_region over [x1, x2] x [y1, y2] (global coordinates),
+   drift along x, with the hooks' plasma (the initial load). */
+int tg_inject_region(tg_ctx *ctx, float x1, float x2, float y1, float y2, float ppc, float weight);
+/* The three hooks as separate calls (the reference's order is tg_move,
+   tg_reset_currents, tg_particle_bc, tg_deposit, ... tg_field_bc ...,
+   tg_inject). */
+int tg_particle_bc(tg_ctx *ctx);
+int tg_field_bc(tg_ctx *ctx);
+int tg_inject(tg_ctx *ctx);
+
+/* ---------------------------------------------------------------------
    Batched ensemble: many independent periodic 2D boxes of uneven size
    (seed or parameter ensembles) stepped together, one launch per phase for
    all boxes, the laps replayed from a captured CUDA graph. No counterpart

@@ -97,6 +97,27 @@ class to_diag(ctypes.Structure):
     ]
 
 
+PDF_SZ = 1000
+
+
+class to_shock(ctypes.Structure):
+    _fields_ = [
+        ("wall", ctypes.c_int32), ("walloc", ctypes.c_double),
+        ("gammawall", ctypes.c_float), ("betawall", ctypes.c_float),
+        ("cond_i1", ctypes.c_int32), ("cond_i2", ctypes.c_int32),
+        ("edge_i1", ctypes.c_int32), ("edge_i2", ctypes.c_int32),
+        ("edge", ctypes.c_float * 6),
+        ("inject", ctypes.c_int32), ("xinject2", ctypes.c_double), ("betainj", ctypes.c_float),
+        ("xinj_max", ctypes.c_double),
+        ("ppc0", ctypes.c_float), ("gamma_drift", ctypes.c_float), ("weight", ctypes.c_float),
+        ("y1", ctypes.c_float), ("y2", ctypes.c_float),
+        ("pcosthmult", ctypes.c_float), ("sigma_nonzero", ctypes.c_int32),
+        ("gamma_table_i", ctypes.c_float * PDF_SZ), ("pdf_table_i", ctypes.c_float * (PDF_SZ + 1)),
+        ("gamma_table_e", ctypes.c_float * PDF_SZ), ("pdf_table_e", ctypes.c_float * (PDF_SZ + 1)),
+        ("dseed", ctypes.c_double), ("totalpartnum", ctypes.c_int32), ("injected", ctypes.c_int64),
+    ]
+
+
 _libs: dict = {}
 _lock = threading.Lock()
 
@@ -127,6 +148,24 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_charge_density.restype = None
             lib.to_num_threads.argtypes = []
             lib.to_num_threads.restype = ctypes.c_int
+            K = ctypes.POINTER(to_shock)
+            lib.to_random.argtypes = [ctypes.POINTER(ctypes.c_double)]
+            lib.to_random.restype = ctypes.c_float
+            lib.to_poisson.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_double)]
+            lib.to_poisson.restype = ctypes.c_float
+            lib.to_sincosf.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+            lib.to_sincosf.restype = None
+            lib.to_init_maxw_table.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_void_p,
+                                               ctypes.c_void_p]
+            lib.to_init_maxw_table.restype = None
+            lib.to_maxwell_dist.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_double)] + \
+                [ctypes.POINTER(ctypes.c_float)] * 3 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_int]
+            lib.to_maxwell_dist.restype = None
+            lib.to_inject_plasma_region.argtypes = [P, K] + [ctypes.c_float] * 6
+            lib.to_inject_plasma_region.restype = None
+            for name in ("to_inject_particles_user", "to_particle_bc_user", "to_field_bc_user", "to_step_shock"):
+                getattr(lib, name).argtypes = [P, K]
+                getattr(lib, name).restype = None
             _libs[path] = lib
         return _libs[path]
 
@@ -220,6 +259,34 @@ class OracleSim:
         out["p_part"] = list(d.p_part)
         out["p_field"] = list(d.p_field)
         return out
+
+    # -- collisionless-shock hooks ------------------------------------------
+    def shock_init(self, sh: dict) -> None:
+        """to_shock from the dict of tristan_gb300.setups.shock_params; the
+        Maxwell-Juttner tables are built by the restatement of
+        init_maxw_table"""
+        k = to_shock()
+        for name, _ in to_shock._fields_:
+            if name in sh and name != "edge":
+                setattr(k, name, sh[name])
+        for a in range(6):
+            k.edge[a] = float(sh["edge"][a])
+        self.lib.to_init_maxw_table(float(sh["delgam_i"]), int(self.cfg.dims), float(sh["pcosthmult"]),
+                                    ctypes.addressof(k.gamma_table_i), ctypes.addressof(k.pdf_table_i))
+        self.lib.to_init_maxw_table(float(sh["delgam_e"]), int(self.cfg.dims), float(sh["pcosthmult"]),
+                                    ctypes.addressof(k.gamma_table_e), ctypes.addressof(k.pdf_table_e))
+        self.shock = k
+        self.kptr = ctypes.pointer(k)
+
+    def inject_region(self, x1, x2, y1, y2, ppc, weight=1.0) -> None:
+        self.lib.to_inject_plasma_region(self.ptr, self.kptr, x1, x2, y1, y2, ppc, weight)
+
+    def step_shock(self, n: int = 1) -> None:
+        for _ in range(n):
+            self.lib.to_step_shock(self.ptr, self.kptr)
+
+    def shock_call(self, name: str) -> None:
+        getattr(self.lib, name)(self.ptr, self.kptr)
 
     def charge_density(self) -> np.ndarray:
         rho = np.zeros(self.lot, np.float64)

@@ -1109,3 +1109,397 @@ void to_diagnostics(const to_state *s, to_diag *out)
     }
     free(rho);
 }
+
+/* ------------------------------------------------------------------------
+ * Collisionless-shock setup, 2D (user_pu/user_shock_pu.F90 with wall = 1,
+ * rightclean = 0, rightwall = 0, wallgam from the input).
+ * --------------------------------------------------------------------- */
+
+/* Park-Miller minimal standard generator, code/aux.F90:82-99: the seed is
+   an integer held in a double, SEED = DMOD(16807*SEED, 2^31-1) (exact in
+   double), returned as SEED/2^31 rounded to single */
+float to_random(double *dseed)
+{
+    double seed = fmod(16807.0 * *dseed, 2147483647.0);
+    *dseed = seed;
+    return (float)(seed / 2147483648.0);
+}
+
+/* code/aux.F90:110-134 */
+float to_poisson(float numps, double *dseed)
+{
+    double Lps = exp(-(double)numps);
+    float kps = 0.0f;
+    double pps = 1.0;
+    while (pps >= Lps) {
+        kps = kps + 1.0f;
+        float ups = to_random(dseed);
+        pps = pps * (double)ups;
+    }
+    return kps - 1.0f;
+}
+
+/* sin and cos of a float: reduction by pi/2 in double (pi/2 split into a
+   33-bit head and a tail, so k * head is exact), Taylor series to degree
+   17 on |r| <= pi/4, one rounding to single at the end */
+static double sin_taylor(double r)
+{
+    const double r2 = r * r;
+    double t = 1.0 / 355687428096000.0;               /* 1/17! */
+    t = 1.0 / 1307674368000.0 - r2 * t;               /* 1/15! */
+    t = 1.0 / 6227020800.0 - r2 * t;                  /* 1/13! */
+    t = 1.0 / 39916800.0 - r2 * t;                    /* 1/11! */
+    t = 1.0 / 362880.0 - r2 * t;                      /* 1/9!  */
+    t = 1.0 / 5040.0 - r2 * t;                        /* 1/7!  */
+    t = 1.0 / 120.0 - r2 * t;                         /* 1/5!  */
+    t = 1.0 / 6.0 - r2 * t;                           /* 1/3!  */
+    return r - r * r2 * t;
+}
+
+static double cos_taylor(double r)
+{
+    const double r2 = r * r;
+    double t = 1.0 / 20922789888000.0;                /* 1/16! */
+    t = 1.0 / 87178291200.0 - r2 * t;                 /* 1/14! */
+    t = 1.0 / 479001600.0 - r2 * t;                   /* 1/12! */
+    t = 1.0 / 3628800.0 - r2 * t;                     /* 1/10! */
+    t = 1.0 / 40320.0 - r2 * t;                       /* 1/8!  */
+    t = 1.0 / 720.0 - r2 * t;                         /* 1/6!  */
+    t = 1.0 / 24.0 - r2 * t;                          /* 1/4!  */
+    t = 0.5 - r2 * t;                                 /* 1/2!  */
+    return 1.0 - r2 * t;
+}
+
+void to_sincosf(float x, float *sn, float *cs)
+{
+    const double PIO2_HI = 0x1.921fb544p+0, PIO2_LO = 0x1.0b4611a626331p-34, TWO_OVER_PI = 0x1.45f306dc9c883p-1;
+    const double xd = (double)x;
+    const double k = nearbyint(xd * TWO_OVER_PI);
+    const double r = (xd - k * PIO2_HI) - k * PIO2_LO;
+    const double s = sin_taylor(r), c = cos_taylor(r);
+    const long q = ((long)k) & 3;
+    double so, co;
+    if (q == 0) { so = s; co = c; }
+    else if (q == 1) { so = c; co = -s; }
+    else if (q == 2) { so = -s; co = -c; }
+    else { so = -c; co = s; }
+    *sn = (float)so;
+    *cs = (float)co;
+}
+
+/* code/particles.F90:2126-2163 */
+void to_init_maxw_table(float delgam, int dims, float pcosthmult, float *gt, float *pt)
+{
+    float maxg = delgam * 20.0f + 1.0f;
+    float func[TO_PDF_SZ];
+    for (int i = 1; i <= TO_PDF_SZ; i++)
+        gt[i - 1] = (maxg - 1.0f) / (float)(TO_PDF_SZ - 1) * (float)(i - 1);
+    for (int i = 0; i < TO_PDF_SZ; i++) {
+        const float g = gt[i];
+        if (dims == 3 || pcosthmult == 1.0f)
+            func[i] = (g + 1.0f) * sqrtf(g * (g + 2.0f)) * expf(-g / delgam);
+        else
+            func[i] = (g + 1.0f) * expf(-g / delgam);
+    }
+    pt[0] = 0.0f;
+    float sum = 0.0f;
+    for (int i = 1; i <= TO_PDF_SZ; i++) {
+        sum = sum + func[i - 1];
+        pt[i] = sum;
+    }
+    /* the whole array divided by its element pdf_sz (1-based), read before
+       the assignment */
+    const float norm = pt[TO_PDF_SZ - 1];
+    for (int i = 0; i <= TO_PDF_SZ; i++) pt[i] = pt[i] / norm;
+}
+
+/* code/particles.F90:2176-2273, 2D build (pcosth drawn once more when
+   sigma != 0); pi is the double of the single literal 3.1415927 */
+void to_maxwell_dist(float gamma0, float cd, double *dseed, float *u, float *v, float *w, const float *gt,
+                     const float *pt, float pcosthmult, int sigma_nonzero)
+{
+    const double pi = (double)3.1415927f;
+    const float gamma0mag = fabsf(gamma0);
+    const float gm = fmaxf(fabsf(gamma0), 1.0f);
+    const float beta_drift = copysignf(sqrtf(1.0f - 1.0f / (gm * gm)), gamma0);
+    float rannum = to_random(dseed);
+    if (rannum == 1.0f) rannum = to_random(dseed);
+    float gam = 0.0f;
+    for (int i = 1;; i++) {
+        int done = 0;
+        if (i == TO_PDF_SZ) {
+            gam = gt[TO_PDF_SZ - 1];
+            done = 1;
+        }
+        if (i < TO_PDF_SZ && rannum >= pt[i - 1] && rannum < pt[i]) {
+            gam = gt[i - 1] + (gt[i] - gt[i - 1]) / (pt[i] - pt[i - 1]) * (rannum - pt[i - 1]);
+            done = 1;
+        }
+        if (done) break;
+    }
+    float pcosth = (2.0f * to_random(dseed) - 1.0f) * pcosthmult;
+    if (sigma_nonzero) pcosth = 2.0f * to_random(dseed) - 1.0f;
+    const float pphi = (float)((double)(to_random(dseed) * 2.0f) * pi);
+    const float psinth = sqrtf(1.0f - pcosth * pcosth);
+    const float v0t = cd * sqrtf(gam * (gam + 2.0f)) / (1.0f + gam);
+    float sphi, cphi;
+    to_sincosf(pphi, &sphi, &cphi);
+    const float ut1 = v0t * psinth * cphi;
+    const float vt1 = v0t * psinth * sphi;
+    const float wt1 = v0t * pcosth;
+    float ptx = (1.0f + gam) * ut1;
+    const float pty = (1.0f + gam) * vt1;
+    const float ptz = (1.0f + gam) * wt1;
+    const float X7 = to_random(dseed);
+    if (-beta_drift * ut1 / cd > X7) ptx = -ptx;
+    const float px1 = (ptx + cd * beta_drift * (gam + 1.0f)) * gamma0mag;
+    *u = px1 / cd;
+    *v = pty / cd;
+    *w = ptz / cd;
+}
+
+/* code/particles.F90:2549-2938 for 2D, drift along x, one electron per ion,
+   no density profile: ions and electrons appended pairwise at one point */
+void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float ppc,
+                             float weight)
+{
+    const int ng = s->nghost, ngz = s->nghostz;
+    const float gdi = k->gamma_drift;
+    const float gamma_drift = fabsf(gdi) < 1.0f ? copysignf(sqrtf(1.0f / (1.0f - gdi * gdi)), gdi) : gdi;
+    const int64_t iglob_min = (ng / 2 + 1) + s->mxcum, iglob_max = (s->mx - ng / 2) + s->mxcum;
+    float minx = (float)(ng / 2 + 1), maxx = (float)(ng / 2 + 1);
+    if (x1 < (float)iglob_min) minx = (float)(ng / 2 + 1);
+    if (x2 < (float)iglob_min) maxx = (float)(ng / 2 + 1);
+    if (x1 >= (float)iglob_max) minx = (float)(s->mx - ng / 2);
+    if (x2 >= (float)iglob_max) maxx = (float)(s->mx - ng / 2);
+    if (x1 >= (float)iglob_min && x1 < (float)iglob_max) minx = x1 - 1.0f * (float)s->mxcum;
+    if (x2 >= (float)iglob_min && x2 < (float)iglob_max) maxx = x2 - 1.0f * (float)s->mxcum;
+    const float delta_x = maxx - minx;
+    const int64_t jglob_min = (ng / 2 + 1) + s->mycum, jglob_max = (s->my - ng / 2) + s->mycum;
+    float miny = (float)(ng / 2 + 1), maxy = (float)(ng / 2 + 1);
+    if (y1 < (float)jglob_min) miny = (float)(ng / 2 + 1);
+    if (y2 < (float)jglob_min) maxy = (float)(ng / 2 + 1);
+    if (y1 >= (float)jglob_max) miny = (float)(s->my - ng / 2);
+    if (y2 >= (float)jglob_max) maxy = (float)(s->my - ng / 2);
+    if (y1 >= (float)jglob_min && y1 < (float)jglob_max) miny = y1 - (float)s->mycum;
+    if (y2 >= (float)jglob_min && y2 < (float)jglob_max) maxy = y2 - (float)s->mycum;
+    float delta_y = maxy - miny;
+    if (maxy == 0.0f || miny == 0.0f) {
+        delta_y = 0.0f;
+        maxy = 0.0f;
+        miny = 0.0f;
+    }
+    const float maxz = 1.0f * (float)(ngz / 2 + 1) + 1.0f, minz = 1.0f * (float)(ngz / 2 + 1);
+    const float delta_z = maxz - minz;
+    float numps = (0.5f * ppc) * delta_z * delta_y * delta_x;
+    if (numps < 10.0f) numps = numps != 0.0f ? to_poisson(numps, &k->dseed) : 0.0f;
+    else numps = (float)(int32_t)ceilf(numps);
+    const int64_t n = (int64_t)(int32_t)numps;
+    if (s->ions + n > s->maxhlf || s->lecs + n > s->maxhlf) {
+        k->injected = -1; /* check_overflow_num would stop the run */
+        return;
+    }
+    for (int64_t m = 0; m < n; m++) {
+        to_particle *pi = &s->p[s->ions++];
+        pi->x = minx + delta_x * to_random(&k->dseed);
+        pi->y = miny + delta_y * to_random(&k->dseed);
+        pi->z = minz + delta_z * to_random(&k->dseed);
+        to_maxwell_dist(gamma_drift, s->c, &k->dseed, &pi->u, &pi->v, &pi->w, k->gamma_table_i, k->pdf_table_i,
+                        k->pcosthmult, k->sigma_nonzero);
+        pi->ch = weight;
+        pi->ind = ++k->totalpartnum;
+        pi->proc = 0;
+        pi->splitlev = 1;
+        to_particle *pe = &s->p[s->maxhlf + s->lecs++];
+        pe->x = pi->x;
+        pe->y = pi->y;
+        pe->z = pi->z;
+        pe->ch = weight / 1.0f;
+        to_maxwell_dist(gamma_drift, s->c, &k->dseed, &pe->u, &pe->v, &pe->w, k->gamma_table_e, k->pdf_table_e,
+                        k->pcosthmult, k->sigma_nonzero);
+        pe->ind = ++k->totalpartnum;
+        pe->proc = 0;
+        pe->splitlev = 1;
+    }
+    k->injected += n;
+}
+
+/* inject_from_wall (code/particles.F90:2439-2538) for a wall normal to x at
+   x1, then the injector's bookkeeping of inject_particles_user
+   (user_shock_pu.F90:364-395 with rightclean = 0, rightwall = 0) */
+void to_inject_particles_user(to_state *s, to_shock *k)
+{
+    k->injected = 0;
+    if (!k->inject) return;
+    const float c = s->c;
+    k->xinject2 = k->xinject2 + (double)(c * k->betainj);
+    if (k->xinject2 > k->xinj_max) {
+        k->xinject2 = k->xinj_max;
+        k->betainj = 0.0f;
+    }
+    const float wall_speed = k->betainj;
+    const float x1 = (float)k->xinject2;
+    const float beta_wall = fabsf(wall_speed) >= 1.0f
+                                ? copysignf(sqrtf(1.0f - 1.0f / (wall_speed * wall_speed)), wall_speed)
+                                : wall_speed;
+    const float gd = k->gamma_drift;
+    const float beta_inj = fabsf(gd) >= 1.0f ? copysignf(sqrtf(1.0f - 1.0f / (gd * gd)), gd) : gd;
+    float x1new = x1, x2new = x1 + (beta_inj - beta_wall) * c;
+    if (x2new < x1new) {
+        const float xt = x1new;
+        x1new = x2new;
+        x2new = xt;
+    }
+    to_inject_plasma_region(s, k, x1new, x2new, k->y1, k->y2, k->ppc0, k->weight);
+    s->x1in = 3.0;
+    s->x2in = k->xinject2;
+}
+
+/* zigzag (code/particles.F90:550-669), 2D: first-order deposit of the
+   segment (x1,y1) -> (x2,y2) through the relay point */
+static void zigzag(to_state *s, const dep_target *t, float x2, float y2, float z2, float x1, float y1, float z1,
+                   float q)
+{
+    const int64_t iy = s->mx;
+    const int i1 = (int)truncf(x1), i2 = (int)truncf(x2);
+    const int j1 = (int)truncf(y1), j2 = (int)truncf(y2);
+    int k1 = (int)truncf(z1), k2 = (int)truncf(z2);
+    const float xr = fminf((float)((i1 < i2 ? i1 : i2) + 1), fmaxf((float)(i1 > i2 ? i1 : i2), 0.5f * (x1 + x2)));
+    const float yr = fminf((float)((j1 < j2 ? j1 : j2) + 1), fmaxf((float)(j1 > j2 ? j1 : j2), 0.5f * (y1 + y2)));
+    const float zr = fminf((float)((k1 < k2 ? k1 : k2) + 1), fmaxf((float)(k1 > k2 ? k1 : k2), 0.5f * (z1 + z2)));
+    k1 = 1;
+    k2 = 1;
+    const float Fx1 = -q * (xr - x1), Fy1 = -q * (yr - y1), Fz1 = -q * (zr - z1);
+    const float Wx1 = 0.5f * (x1 + xr) - (float)i1, Wy1 = 0.5f * (y1 + yr) - (float)j1;
+    const float Wx2 = 0.5f * (x2 + xr) - (float)i2, Wy2 = 0.5f * (y2 + yr) - (float)j2;
+    const float Fx2 = -q * (x2 - xr), Fy2 = -q * (y2 - yr), Fz2 = -q * (z2 - zr);
+    const float Wz1 = 0.0f, Wz2 = 0.0f;
+#define ZL(i, j) ((int64_t)((i) - 1) + iy * (int64_t)((j) - 1))
+    (void)k1; (void)k2;
+    dep_add(t, 0, ZL(i1, j1), Fx1 * (1.0f - Wy1) * (1.0f - Wz1));
+    dep_add(t, 0, ZL(i1, j1 + 1), Fx1 * Wy1 * (1.0f - Wz1));
+    dep_add(t, 0, ZL(i2, j2), Fx2 * (1.0f - Wy2) * (1.0f - Wz2));
+    dep_add(t, 0, ZL(i2, j2 + 1), Fx2 * Wy2 * (1.0f - Wz2));
+    dep_add(t, 1, ZL(i1, j1), Fy1 * (1.0f - Wx1) * (1.0f - Wz1));
+    dep_add(t, 1, ZL(i1 + 1, j1), Fy1 * Wx1 * (1.0f - Wz1));
+    dep_add(t, 1, ZL(i2, j2), Fy2 * (1.0f - Wx2) * (1.0f - Wz2));
+    dep_add(t, 1, ZL(i2 + 1, j2), Fy2 * Wx2 * (1.0f - Wz2));
+    dep_add(t, 2, ZL(i1, j1), Fz1 * (1.0f - Wx1) * (1.0f - Wy1));
+    dep_add(t, 2, ZL(i1 + 1, j1), Fz1 * Wx1 * (1.0f - Wy1));
+    dep_add(t, 2, ZL(i1, j1 + 1), Fz1 * (1.0f - Wx1) * Wy1);
+    dep_add(t, 2, ZL(i1 + 1, j1 + 1), Fz1 * Wx1 * Wy1);
+    dep_add(t, 2, ZL(i2, j2), Fz2 * (1.0f - Wx2) * (1.0f - Wy2));
+    dep_add(t, 2, ZL(i2 + 1, j2), Fz2 * Wx2 * (1.0f - Wy2));
+    dep_add(t, 2, ZL(i2, j2 + 1), Fz2 * (1.0f - Wx2) * Wy2);
+    dep_add(t, 2, ZL(i2 + 1, j2 + 1), Fz2 * Wx2 * Wy2);
+#undef ZL
+}
+
+/* left reflecting wall, user_shock_pu.F90:514-611: a particle found behind
+   the wall is traced back to the crossing, deposits its path up to the
+   wall (zigzag), is reflected with the wall's kick and moved forward for
+   the rest of the step, and the behind-the-wall path that the deposit will
+   add is cancelled (zigzag with -q); a particle that cannot have crossed
+   this step is removed (the last particle of the species takes its slot) */
+void to_particle_bc_user(to_state *s, to_shock *k)
+{
+    if (!k->wall) return;
+    const float c = s->c;
+    const float gammawall = k->gammawall, betawall = k->betawall;
+    k->walloc = k->walloc + (double)(betawall * c);
+    dep_target t = make_target(s);
+    for (int iter = 0; iter < 2; iter++) {
+        const int64_t base = iter == 0 ? 0 : s->maxhlf;
+        int64_t *cnt = iter == 0 ? &s->ions : &s->lecs;
+        const float q0 = iter == 0 ? s->qi : s->qe;
+        int64_t i1 = *cnt;
+        int64_t n1 = 0;
+        while (n1 < i1) {
+            to_particle *p = &s->p[base + n1];
+            if ((double)(p->x + (float)s->mxcum) < k->walloc) {
+                float gamma = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+                const float x0 = p->x - p->u / gamma * c;
+                const float y0 = p->y, z0 = p->z;
+                const double walloc0 = k->walloc - (double)(betawall * c) - (double)s->mxcum;
+                float tfrac = (float)fabs(((double)x0 - walloc0) / (double)(betawall * c - p->u / gamma * c));
+                if (tfrac < 1.0f) {
+                    const float xcolis = x0 + p->u / gamma * c * tfrac;
+                    const float ycolis = y0, zcolis = z0;
+                    float q = p->ch * q0;
+                    zigzag(s, &t, xcolis, ycolis, zcolis, x0, y0, z0, q);
+                    p->u = gammawall * gammawall * gamma * (2.0f * betawall - p->u / gamma * (1.0f + betawall * betawall));
+                    gamma = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+                    tfrac = fminf(fabsf((p->x - xcolis) / fmaxf(fabsf(p->x - x0), 1e-9f)), 1.0f);
+                    p->x = xcolis + p->u / gamma * c * tfrac;
+                    p->y = ycolis;
+                    p->z = zcolis;
+                    q = -q;
+                    zigzag(s, &t, xcolis, ycolis, zcolis, p->x - p->u / gamma * c, p->y - p->v / gamma * c,
+                           p->z - p->w / gamma * c, q);
+                } else {
+                    s->p[base + n1] = s->p[base + i1 - 1];
+                    i1--;
+                    continue;
+                }
+            }
+            n1++;
+        }
+        *cnt = i1;
+    }
+}
+
+/* user_shock_pu.F90:460-488 (rightclean = 0): conductor behind the wall,
+   upstream fields at the right edge */
+void to_field_bc_user(to_state *s, const to_shock *k)
+{
+    const int64_t iy = s->mx, iz = (int64_t)s->mx * s->my;
+    for (int kk = 1; kk <= s->mz; kk++)
+        for (int j = 1; j <= s->my; j++) {
+            const int64_t row = iy * (j - 1) + iz * (kk - 1);
+            if (k->cond_i1 != k->cond_i2)
+                for (int i = k->cond_i1; i <= k->cond_i2; i++) {
+                    s->ey[row + i - 1] = 0.0f;
+                    s->ez[row + i - 1] = 0.0f;
+                }
+            if (k->edge_i1 != k->edge_i2)
+                for (int i = k->edge_i1; i <= k->edge_i2; i++) {
+                    s->bx[row + i - 1] = k->edge[3];
+                    s->by[row + i - 1] = k->edge[4];
+                    s->bz[row + i - 1] = k->edge[5];
+                    s->ex[row + i - 1] = k->edge[0];
+                    s->ey[row + i - 1] = k->edge[1];
+                    s->ez[row + i - 1] = k->edge[2];
+                }
+        }
+}
+
+/* code/tristanmainloop.F90:117-303 with the user hooks (no radiation
+   boundaries: bc_b2 / bc_e2 are bc_b1 / bc_e1) */
+void to_step_shock(to_state *s, to_shock *k)
+{
+    to_bc_b1(s);
+    to_bc_e1(s);
+    to_advance_b_halfstep(s);
+    to_bc_b1(s);
+    to_move_particles(s);
+    to_advance_b_halfstep(s);
+    to_bc_b1(s);
+    to_bc_b1(s);
+    to_field_bc_user(s, k);
+    to_advance_e_fullstep(s);
+    to_field_bc_user(s, k);
+    to_bc_e1(s);
+    to_field_bc_user(s, k);
+    to_reset_currents(s);
+    to_particle_bc_user(s, k);
+    to_bc_e1(s);
+    to_bc_b1(s);
+    to_deposit_particles(s);
+    to_exchange_current(s);
+    to_apply_filter1_opt(s);
+    to_add_current(s);
+    to_field_bc_user(s, k);
+    to_inject_particles_user(s, k);
+    to_reorder_particles(s);
+    s->lap++;
+}

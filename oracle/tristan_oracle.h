@@ -151,6 +151,59 @@ void to_diagnostics(const to_state *s, to_diag *out);
 /* threads used by the OpenMP build (1 in the serial build) */
 int to_num_threads(void);
 
+/* ------------------------------------------------------------------------
+ * Collisionless-shock setup, 2D (user_pu/user_shock_pu.F90): reflecting
+ * left wall with zigzag partial deposits, conductor behind the wall and
+ * right-edge field reset, moving injector; the Park-Miller generator
+ * (code/aux.F90:82-134) and the Maxwell-Juttner loader
+ * (code/particles.F90:2126-2273, :2439-2938).
+ * --------------------------------------------------------------------- */
+#define TO_PDF_SZ 1000
+
+typedef struct {
+    /* left wall (particle_bc_user, user_shock_pu.F90:514-611) */
+    int32_t wall;
+    double walloc;          /* wall position (global x) */
+    float gammawall, betawall;
+    /* field_bc_user (user_shock_pu.F90:460-488): ey = ez = 0 on local
+       i = cond_i1..cond_i2, and the upstream fields written on
+       i = edge_i1..edge_i2 */
+    int32_t cond_i1, cond_i2, edge_i1, edge_i2;
+    float edge[6];          /* ex ey ez bx by bz */
+    /* moving injector (inject_particles_user, :364-395) */
+    int32_t inject;
+    double xinject2;
+    float betainj;
+    double xinj_max;        /* mx0 - 15 */
+    float ppc0, gamma_drift, weight;
+    float y1, y2;           /* injection band, global y */
+    /* Maxwell-Juttner loader */
+    float pcosthmult;
+    int32_t sigma_nonzero;
+    float gamma_table_i[TO_PDF_SZ], pdf_table_i[TO_PDF_SZ + 1];
+    float gamma_table_e[TO_PDF_SZ], pdf_table_e[TO_PDF_SZ + 1];
+    double dseed;
+    int32_t totalpartnum;
+    int64_t injected;       /* pairs injected by the last call */
+} to_shock;
+
+float to_random(double *dseed);                                   /* aux.F90:82-99 */
+float to_poisson(float numps, double *dseed);                     /* aux.F90:110-134 */
+void to_init_maxw_table(float delgam, int dims, float pcosthmult, float *gamma_table, float *pdf_table);
+void to_maxwell_dist(float gamma0, float cd, double *dseed, float *u, float *v, float *w,
+                     const float *gamma_table, const float *pdf_table, float pcosthmult, int sigma_nonzero);
+/* inject_plasma_region for 2D, drift along x (direction 1) */
+void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float ppc,
+                             float weight);
+void to_inject_particles_user(to_state *s, to_shock *k);          /* :364-395 */
+void to_particle_bc_user(to_state *s, to_shock *k);               /* :514-611 */
+void to_field_bc_user(to_state *s, const to_shock *k);            /* :460-488 */
+/* the shock's lap: the periodic lap with the user hooks at their places
+   in code/tristanmainloop.F90:117-303 */
+void to_step_shock(to_state *s, to_shock *k);
+/* sin and cos of a float argument, evaluated in double and rounded once */
+void to_sincosf(float x, float *sn, float *cs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,7 +24,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
-           "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-I", INCLUDE]
+           "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
+           "-I", INCLUDE]
 
 
 def nvcc() -> str:

@@ -49,6 +49,9 @@ class SimConfig:
     sort_every: int = 1
     tile: tuple = (0, 0, 0)
     diag_every: int = 0
+    # open-boundary window (x1in, x2in, y1in, y2in, z1in, z2in) when a
+    # problem setup sets its own (None: the one allocate_particles derives)
+    window: tuple | None = None
 
     # -- derived grid ----------------------------------------------------
     @property
@@ -126,6 +129,8 @@ class SimConfig:
     def window_in(self):
         """x1in..z2in of allocate_particles (code/particles.F90:335-340);
         the reference's mx0 there already includes the ghosts."""
+        if self.window is not None:
+            return tuple(float(v) for v in self.window)
         ng, ngz = self.nghost, self.nghostz
         return (float(ng // 2 + 1), float(self.mx - ng // 2),
                 float(ng // 2 + 1), float(self.my - ng // 2),

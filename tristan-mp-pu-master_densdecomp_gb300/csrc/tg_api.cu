@@ -67,6 +67,12 @@ struct tg_ctx {
     bool ev_used[65][TG_NPHASES] = {};
     long long lap = 0;
     long long lapreorder = 0;
+    // collisionless-shock hooks
+    bool shock_on = false;
+    ShockParams K;
+    ShockState *d_shock = nullptr;
+    float *d_tables = nullptr;  // gt_i, pt_i, gt_e, pt_e
+    tg_shock hshock;
     char err[512] = {0};
     std::vector<void *> allocs;
 };
@@ -353,12 +359,19 @@ extern "C" int32_t tg_kernels_per_step(tg_ctx *ctx) { return ctx ? ctx->kernels_
 // tile sort: count (unless the tile kernel already did), scan, scatter,
 // flip parity
 // ---------------------------------------------------------------------------
+// grid-size hint for kernels that read the particle count on the device:
+// the host's count, or the capacity when device-side injection may have
+// grown it since
+static long long count_hint(const tg_ctx *ctx, int s) {
+    return ctx->shock_on ? (long long)ctx->cfg.maxhlf : ctx->hcount[s];
+}
+
 static int sort_species(tg_ctx *ctx, int s, bool counted) {
     const int p = ctx->par;
     long long *cnt_cur = ctx->d_cnt + 2 * p + s, *cnt_next = ctx->d_cnt + 2 * (1 - p) + s;
-    if (!counted) CK(launch_tile_count(ctx->g, ctx->sp[p][s], cnt_cur, ctx->hcount[s], ctx->hist[s], ctx->st));
+    if (!counted) CK(launch_tile_count(ctx->g, ctx->sp[p][s], cnt_cur, count_hint(ctx, s), ctx->hist[s], ctx->st));
     CK(launch_scan(ctx->hist[s], ctx->tstart[s], ctx->cursor[s], ctx->g.ntiles, cnt_next, ctx->st));
-    CK(launch_scatter(ctx->g, ctx->sp[p][s], ctx->sp[1 - p][s], cnt_cur, ctx->hcount[s], ctx->tstart[s],
+    CK(launch_scatter(ctx->g, ctx->sp[p][s], ctx->sp[1 - p][s], cnt_cur, count_hint(ctx, s), ctx->tstart[s],
                       ctx->cursor[s], ctx->st));
     return TG_OK;
 }
@@ -397,6 +410,12 @@ static TileArgs tile_args(tg_ctx *ctx, bool count_tiles) {
         a.fix[cc] = ctx->fix[cc];
     }
     a.status = ctx->d_status;
+    if (ctx->shock_on) {
+        a.shock = ctx->d_shock;
+        a.wall = ctx->K.wall;
+        a.gammawall = ctx->K.gammawall;
+        a.betawall = ctx->K.betawall;
+    }
     return a;
 }
 
@@ -548,7 +567,7 @@ extern "C" int tg_move(tg_ctx *ctx) {
     if (ctx->g.dims == 3) CK(launch_primal(ctx->g, ctx->f, ctx->prim, ctx->st));
     for (int s = 0; s < 2; s++)
         CK(launch_push_flat(ctx->g, ctx->P, fp, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,
-                            ctx->hcount[s], ctx->P.qm[s], ctx->d_status, ctx->st));
+                            count_hint(ctx, s), ctx->P.qm[s], ctx->d_status, ctx->st));
     ctx->dirty = true;
     ctx->may_have_dead = true;
     return TG_OK;
@@ -706,6 +725,196 @@ extern "C" int tg_diag_history(tg_ctx *ctx, double *out, int32_t n) {
 }
 
 // ---------------------------------------------------------------------------
+// collisionless-shock hooks
+// ---------------------------------------------------------------------------
+static const int INJECT_GRID = 152 * 4;
+
+// init_maxw_table (code/particles.F90:2126-2163) on the host, as the
+// reference evaluates it (single precision, sequential sums, normalised by
+// the element pdf_sz read before the assignment)
+static void maxw_table(float delgam, int dims, float pcosthmult, float *gt, float *pt) {
+    const float maxg = delgam * 20.0f + 1.0f;
+    std::vector<float> func(TG_PDF_SZ);
+    for (int i = 1; i <= TG_PDF_SZ; i++) gt[i - 1] = (maxg - 1.0f) / (float)(TG_PDF_SZ - 1) * (float)(i - 1);
+    for (int i = 0; i < TG_PDF_SZ; i++) {
+        const float g = gt[i];
+        if (dims == 3 || pcosthmult == 1.0f) func[i] = (g + 1.0f) * sqrtf(g * (g + 2.0f)) * expf(-g / delgam);
+        else func[i] = (g + 1.0f) * expf(-g / delgam);
+    }
+    pt[0] = 0.0f;
+    float sum = 0.0f;
+    for (int i = 1; i <= TG_PDF_SZ; i++) {
+        sum = sum + func[i - 1];
+        pt[i] = sum;
+    }
+    const float norm = pt[TG_PDF_SZ - 1];
+    for (int i = 0; i <= TG_PDF_SZ; i++) pt[i] = pt[i] / norm;
+}
+
+static long long host_powmod31(long long a, long long e) {
+    unsigned long long r = 1, b = (unsigned long long)a;
+    while (e > 0) {
+        if (e & 1) r = (r * b) % 2147483647ULL;
+        b = (b * b) % 2147483647ULL;
+        e >>= 1;
+    }
+    return (long long)r;
+}
+
+extern "C" int tg_shock_init(tg_ctx *ctx, const tg_shock *k) {
+    if (!ctx || !k) return TG_ERR_ARG;
+    if (ctx->g.dims != 2) return fail(ctx, TG_ERR_ARG, "tg_shock_init: the shock hooks are 2D");
+    if (ctx->cfg.sort_every > 1)
+        return fail(ctx, TG_ERR_ARG, "tg_shock_init: injection needs a tile sort every lap (sort_every = 1)");
+    if (k->dseed < 1.0 || k->dseed >= 2147483647.0 || k->dseed != floor(k->dseed))
+        return fail(ctx, TG_ERR_ARG, "tg_shock_init: dseed must be an integer in [1, 2^31 - 2]");
+    std::vector<float> tab(4 * (TG_PDF_SZ + 1));
+    float *gti = tab.data(), *pti = gti + (TG_PDF_SZ + 1), *gte = pti + (TG_PDF_SZ + 1), *pte = gte + (TG_PDF_SZ + 1);
+    maxw_table(k->delgam_i, ctx->g.dims, k->pcosthmult, gti, pti);
+    maxw_table(k->delgam_e, ctx->g.dims, k->pcosthmult, gte, pte);
+    if (!ctx->d_tables) {
+        int r = dalloc(ctx, &ctx->d_tables, tab.size());
+        if (!r) r = dalloc(ctx, &ctx->d_shock, 1);
+        if (r) return r;
+    }
+    ShockParams K;
+    memset(&K, 0, sizeof K);
+    K.wall = k->wall;
+    K.inject = k->inject;
+    K.gammawall = k->gammawall;
+    K.betawall = k->betawall;
+    K.cond_i1 = k->cond_i1;
+    K.cond_i2 = k->cond_i2;
+    K.edge_i1 = k->edge_i1;
+    K.edge_i2 = k->edge_i2;
+    for (int a = 0; a < 6; a++) K.edge[a] = k->edge[a];
+    K.xinj_max = k->xinj_max;
+    K.ppc0 = k->ppc0;
+    K.gamma_drift = k->gamma_drift;
+    K.weight = k->weight;
+    K.y1 = k->y1;
+    K.y2 = k->y2;
+    K.pcosthmult = k->pcosthmult;
+    K.sigma_nonzero = k->sigma_nonzero;
+    const size_t T = TG_PDF_SZ + 1;
+    K.gt[0] = ctx->d_tables;
+    K.pt[0] = ctx->d_tables + T;
+    K.gt[1] = ctx->d_tables + 2 * T;
+    K.pt[1] = ctx->d_tables + 3 * T;
+    K.a13 = host_powmod31(16807, 13);
+    if (K.cond_i1 != K.cond_i2 && (K.cond_i1 < 1 || K.cond_i2 > ctx->g.mx || K.cond_i1 > K.cond_i2))
+        return fail(ctx, TG_ERR_ARG, "tg_shock_init: conductor columns outside [1, mx]");
+    if (K.edge_i1 != K.edge_i2 && (K.edge_i1 < 1 || K.edge_i2 > ctx->g.mx || K.edge_i1 > K.edge_i2))
+        return fail(ctx, TG_ERR_ARG, "tg_shock_init: edge columns outside [1, mx]");
+    ShockState S;
+    memset(&S, 0, sizeof S);
+    S.xinject2 = k->xinject2;
+    S.walloc = k->walloc;
+    S.x2in = ctx->P.x2in;
+    S.betainj = k->betainj;
+    S.totalpartnum = k->totalpartnum;
+    S.seed = (long long)k->dseed;
+    S.weight = k->weight;
+    CK(cudaMemcpyAsync(ctx->d_tables, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d_shock, &S, sizeof S, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->K = K;
+    ctx->hshock = *k;
+    ctx->shock_on = true;
+    for (int p = 0; p < 2; p++)
+        if (ctx->cycle[p]) {
+            cudaGraphExecDestroy(ctx->cycle[p]);
+            ctx->cycle[p] = nullptr;
+        }
+    return TG_OK;
+}
+
+extern "C" int tg_shock_get(tg_ctx *ctx, tg_shock *out) {
+    if (!ctx || !out) return TG_ERR_ARG;
+    if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_shock_get: hooks not set");
+    ShockState S;
+    CK(cudaMemcpyAsync(&S, ctx->d_shock, sizeof S, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *out = ctx->hshock;
+    out->xinject2 = S.xinject2;
+    out->walloc = S.walloc;
+    out->betainj = S.betainj;
+    out->dseed = (double)S.seed;
+    out->totalpartnum = S.totalpartnum;
+    return check_status(ctx);
+}
+
+static const Species *cur_species(tg_ctx *ctx) { return ctx->sp[ctx->par]; }
+
+// one injection: plan, a parallel pass over the pairs, finish; host-driven
+// loads (lap = false) re-run the pass after a gamma redraw when many pairs
+// follow it, so the finishing kernel's sequential tail stays short
+static int inject_run(tg_ctx *ctx, int mode, float x1, float x2, float y1, float y2, float ppc, float weight,
+                      bool in_lap, int *const *hist) {
+    long long *cnt = ctx->d_cnt + 2 * ctx->par;
+    CK(launch_inject_plan(ctx->g, ctx->P, ctx->K, ctx->d_shock, mode, x1, x2, y1, y2, ppc, weight, cnt,
+                          ctx->cfg.maxhlf, ctx->d_status, ctx->st));
+    CK(launch_inject_pairs(ctx->g, ctx->P, ctx->K, ctx->d_shock, cur_species(ctx), INJECT_GRID, ctx->d_status,
+                           ctx->st));
+    if (!in_lap) {
+        for (;;) {
+            ShockState S;
+            CK(cudaMemcpyAsync(&S, ctx->d_shock, sizeof S, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
+            if (S.first_redraw >= S.n || S.n - S.first_redraw <= 4096) break;
+            CK(launch_inject_fixup(ctx->g, ctx->P, ctx->K, ctx->d_shock, ctx->st));
+            CK(launch_inject_pairs(ctx->g, ctx->P, ctx->K, ctx->d_shock, cur_species(ctx), INJECT_GRID,
+                                   ctx->d_status, ctx->st));
+        }
+    }
+    CK(launch_inject_finish(ctx->g, ctx->P, ctx->K, ctx->d_shock, cur_species(ctx), cnt, hist, INJECT_GRID,
+                            ctx->d_status, ctx->st));
+    return TG_OK;
+}
+
+static int inject_lap(tg_ctx *ctx, bool sort_now) {
+    return inject_run(ctx, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, true, sort_now ? ctx->hist : nullptr);
+}
+
+extern "C" int tg_inject_region(tg_ctx *ctx, float x1, float x2, float y1, float y2, float ppc, float weight) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_inject_region: hooks not set (tg_shock_init)");
+    if (!(x2 >= x1) || !(y2 >= y1)) return fail(ctx, TG_ERR_ARG, "tg_inject_region: x2 < x1 or y2 < y1");
+    int r = inject_run(ctx, 1, x1, x2, y1, y2, ppc, weight, false, nullptr);
+    if (r) return r;
+    ctx->dirty = true;
+    ctx->may_have_dead = true;
+    return check_status(ctx);
+}
+
+extern "C" int tg_inject(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_inject: hooks not set (tg_shock_init)");
+    int r = inject_run(ctx, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false, nullptr);
+    if (r) return r;
+    ctx->dirty = true;
+    ctx->may_have_dead = true;
+    return TG_OK;
+}
+
+extern "C" int tg_particle_bc(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_particle_bc: hooks not set (tg_shock_init)");
+    float *cur3[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
+    CK(launch_particle_bc(ctx->g, ctx->P, ctx->K, ctx->d_shock, cur_species(ctx), ctx->d_cnt + 2 * ctx->par,
+                          count_hint(ctx, 0) + count_hint(ctx, 1), cur3, ctx->fix, ctx->d_status, ctx->st));
+    ctx->may_have_dead = true;
+    return TG_OK;
+}
+
+extern "C" int tg_field_bc(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_field_bc: hooks not set (tg_shock_init)");
+    CK(launch_field_bc(ctx->g, ctx->K, ctx->f, ctx->st));
+    return TG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // fused lap
 // ---------------------------------------------------------------------------
 static cudaError_t mark(tg_ctx *ctx, int li, int phase, int end) {
@@ -733,14 +942,21 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
     CK(mark(ctx, li, 0, 1));
     CK(mark(ctx, li, 1, 0));
     TileArgs a = tile_args(ctx, sort_now);
+    // particle_bc_user (the wall) runs inside the tile kernel, between the
+    // push and the deposit; the wall advances first
+    if (ctx->shock_on && ctx->K.wall) { CK(launch_wall_step(ctx->P, ctx->K, ctx->d_shock, st)); k++; }
     CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++;
     CK(mark(ctx, li, 1, 1));
     CK(mark(ctx, li, 2, 0));
-    // advance_Bhalfstep; bc_b1; bc_b2 (:139-145); advance_Efield; bc_e2
+    // advance_Bhalfstep; bc_b1; bc_b2 (:139-145); [field_bc_user];
+    // advance_Efield; [field_bc_user]; bc_e2; [field_bc_user]
     CK(launch_advance_b(g, ctx->P, ctx->f, st)); k++;
     CK(launch_ghost(g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, st)); k++;
+    if (ctx->shock_on) { CK(launch_field_bc(g, ctx->K, ctx->f, st)); k++; }
     CK(launch_advance_e(g, ctx->P, ctx->f, st)); k++;
+    if (ctx->shock_on) { CK(launch_field_bc(g, ctx->K, ctx->f, st)); k++; }
     CK(launch_ghost(g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, st)); k++;
+    if (ctx->shock_on) { CK(launch_field_bc(g, ctx->K, ctx->f, st)); k++; }
     CK(mark(ctx, li, 2, 1));
     CK(mark(ctx, li, 3, 0));
     if (ctx->P.fixed) {
@@ -753,6 +969,14 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
     if (r) return r;
     k += ctx->cfg.ntimes;
     CK(launch_add_current(g, ctx->f, st)); k++;
+    if (ctx->shock_on) {
+        // field_bc_user; inject_particles_user (:242-262); the injected
+        // particles join the tile histogram of this lap's sort
+        CK(launch_field_bc(g, ctx->K, ctx->f, st)); k++;
+        int rr = inject_lap(ctx, sort_now);
+        if (rr) return rr;
+        k += 4;
+    }
     CK(mark(ctx, li, 3, 1));
     if (sort_now) {
         CK(mark(ctx, li, 4, 0));

@@ -331,7 +331,8 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
 // Returns false when the particle is discarded.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__device__ __forceinline__ bool wrap_particle(const Geom &g, const Params &P, float &x, float &y, float &z) {
+__device__ __forceinline__ bool wrap_particle(const Geom &g, const Params &P, float &x, float &y, float &z,
+                                              double x2in) {
     const float midx = 0.5f * (g.maxx - g.minx), midy = 0.5f * (g.maxy - g.miny), midz = 0.5f * (g.maxz - g.minz);
     float perx = 0.0f, pery = 0.0f, perz = 0.0f;
     if (x < g.minx || x > g.maxx) perx = copysignf(midx, x - g.minx) + copysignf(midx, x - g.maxx);
@@ -340,7 +341,7 @@ __device__ __forceinline__ bool wrap_particle(const Geom &g, const Params &P, fl
     bool in = true;
     if (!g.per[0]) {
         float xg = x + (float)P.mxcum;
-        in = ((double)xg > P.x1in) && ((double)xg < P.x2in);
+        in = ((double)xg > P.x1in) && ((double)xg < x2in);
     }
     if (!g.per[1] && in) {
         float yg = y + (float)P.mycum;
@@ -360,6 +361,38 @@ __device__ __forceinline__ bool wrap_particle(const Geom &g, const Params &P, fl
     return in;
 }
 
+// ---------------------------------------------------------------------------
+// collisionless-shock hooks (tg_shock.cu)
+// ---------------------------------------------------------------------------
+#define TG_PDF_SZ 1000
+// state the hooks update on the device (one per context)
+struct ShockState {
+    double xinject2, walloc, x2in;
+    float betainj;
+    int totalpartnum;
+    long long seed;  // Park-Miller state, an integer in [1, 2^31 - 2]
+    // the current injection: region, pairs, first pair of the running pass
+    float minx, delta_x, miny, delta_y, minz, delta_z;
+    int n, k0;
+    long long seed_k0;
+    int first_redraw;  // first pair of the pass whose gamma draw was redrawn (n: none)
+    long long base[2];  // particle counts before the injection
+    float weight;
+};
+// constants of the hooks
+struct ShockParams {
+    int wall, inject;
+    float gammawall, betawall;
+    int cond_i1, cond_i2, edge_i1, edge_i2;
+    float edge[6];
+    double xinj_max;
+    float ppc0, gamma_drift, weight, y1, y2;
+    float pcosthmult;
+    int sigma_nonzero;
+    const float *gt[2], *pt[2];  // Maxwell-Juttner tables of ions and electrons (device)
+    long long a13;               // 16807^13 mod (2^31 - 1): one pair without redraws
+};
+
 // arguments of the tile kernel (particles sorted by tile)
 struct TileArgs {
     Geom g;
@@ -371,6 +404,11 @@ struct TileArgs {
     float *cur[3];
     unsigned long long *fix[3];
     int *status;
+    // shock hooks (null: none): the moving open boundary x2in and, with
+    // wall != 0, the reflecting wall and its constants
+    const ShockState *shock;
+    int wall;
+    float gammawall, betawall;
 };
 
 // ---------------------------------------------------------------------------
@@ -421,6 +459,32 @@ struct DiagLaunch {
     bool particles;  // false: the lap's tile kernel already summed the particles
 };
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
+
+// shock hooks (tg_shock.cu)
+cudaError_t launch_field_bc(const Geom &g, const ShockParams &K, float *const *f, cudaStream_t st);
+// the wall's advance for this lap (before the push)
+cudaError_t launch_wall_step(const Params &P, const ShockParams &K, ShockState *S, cudaStream_t st);
+// wall advance and the wall over all particles (particle_bc_user alone)
+cudaError_t launch_particle_bc(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
+                               const Species *sp, const long long *count, long long hint, float *const *cur,
+                               unsigned long long *const *fix, int *status, cudaStream_t st);
+// plan one injection: mode 0 = the moving injector's slab, 1 = the region
+// (x1, x2, y1, y2) with ppc and weight
+cudaError_t launch_inject_plan(const Geom &g, const Params &P, const ShockParams &K, ShockState *S, int mode,
+                               float x1, float x2, float y1, float y2, float ppc, float weight,
+                               const long long *count, long long maxhlf, int *status, cudaStream_t st);
+// one parallel pass over the pairs [k0, n) of the plan
+cudaError_t launch_inject_pairs(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
+                                const Species *sp, int grid, int *status, cudaStream_t st);
+// after a pass with a redraw at pair kf: the next pass starts at kf + 1
+cudaError_t launch_inject_fixup(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
+                                cudaStream_t st);
+// finish: pairs after a remaining redraw sequentially, generator state,
+// ind counter, particle counts; then (hist non-null) the new particles'
+// tile histogram
+cudaError_t launch_inject_finish(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
+                                 const Species *sp, long long *count, int *const *hist, int grid, int *status,
+                                 cudaStream_t st);
 
 // launchers (tg_fields.cu); fields f[9] = ex ey ez bx by bz curx cury curz
 enum GhostKind { GHOST_BC = 0, GHOST_FILTER = 1 };

@@ -77,7 +77,9 @@ __device__ __forceinline__ void store_pos(const Geom &g, const Species &s, long 
     s.oz[n] = DIM == 3 ? z - (float)k : z;
 }
 
-// warp-aggregated atomicAdd of 1 to counter[key]; returns this lane's slot
+// warp-aggregated atomicAdd of 1 to counter[key]; returns this lane's slot.
+// Lanes are grouped by key alone: every active lane must pass the same
+// counter array.
 __device__ __forceinline__ int agg_inc(int *counter, int key) {
     const unsigned active = __activemask();
     const unsigned peers = __match_any_sync(active, key);
@@ -173,6 +175,71 @@ struct WindowSink {
         }
     }
 };
+
+// ---------------------------------------------------------------------------
+// zigzag (code/particles.F90:550-669), 2D: first-order current of the
+// segment (x1,y1) -> (x2,y2) split at the relay point (Umeda et al. 2003);
+// the wall's partial deposits use it whatever the shape order
+// ---------------------------------------------------------------------------
+template <class Sink>
+__device__ __forceinline__ void zigzag(Sink &sink, float x2, float y2, float z2, float x1, float y1, float z1,
+                                       float q) {
+    const int i1 = (int)truncf(x1), i2 = (int)truncf(x2);
+    const int j1 = (int)truncf(y1), j2 = (int)truncf(y2);
+    const int k1 = (int)truncf(z1), k2 = (int)truncf(z2);
+    const float xr = fminf((float)(min(i1, i2) + 1), fmaxf((float)max(i1, i2), 0.5f * (x1 + x2)));
+    const float yr = fminf((float)(min(j1, j2) + 1), fmaxf((float)max(j1, j2), 0.5f * (y1 + y2)));
+    const float zr = fminf((float)(min(k1, k2) + 1), fmaxf((float)max(k1, k2), 0.5f * (z1 + z2)));
+    const float Fx1 = -q * (xr - x1), Fy1 = -q * (yr - y1), Fz1 = -q * (zr - z1);
+    const float Wx1 = 0.5f * (x1 + xr) - (float)i1, Wy1 = 0.5f * (y1 + yr) - (float)j1;
+    const float Wx2 = 0.5f * (x2 + xr) - (float)i2, Wy2 = 0.5f * (y2 + yr) - (float)j2;
+    const float Fx2 = -q * (x2 - xr), Fy2 = -q * (y2 - yr), Fz2 = -q * (z2 - zr);
+    const float Wz1 = 0.0f, Wz2 = 0.0f;
+    sink.add(0, i1, j1, 1, Fx1 * (1.0f - Wy1) * (1.0f - Wz1));
+    sink.add(0, i1, j1 + 1, 1, Fx1 * Wy1 * (1.0f - Wz1));
+    sink.add(0, i2, j2, 1, Fx2 * (1.0f - Wy2) * (1.0f - Wz2));
+    sink.add(0, i2, j2 + 1, 1, Fx2 * Wy2 * (1.0f - Wz2));
+    sink.add(1, i1, j1, 1, Fy1 * (1.0f - Wx1) * (1.0f - Wz1));
+    sink.add(1, i1 + 1, j1, 1, Fy1 * Wx1 * (1.0f - Wz1));
+    sink.add(1, i2, j2, 1, Fy2 * (1.0f - Wx2) * (1.0f - Wz2));
+    sink.add(1, i2 + 1, j2, 1, Fy2 * Wx2 * (1.0f - Wz2));
+    sink.add(2, i1, j1, 1, Fz1 * (1.0f - Wx1) * (1.0f - Wy1));
+    sink.add(2, i1 + 1, j1, 1, Fz1 * Wx1 * (1.0f - Wy1));
+    sink.add(2, i1, j1 + 1, 1, Fz1 * (1.0f - Wx1) * Wy1);
+    sink.add(2, i1 + 1, j1 + 1, 1, Fz1 * Wx1 * Wy1);
+    sink.add(2, i2, j2, 1, Fz2 * (1.0f - Wx2) * (1.0f - Wy2));
+    sink.add(2, i2 + 1, j2, 1, Fz2 * Wx2 * (1.0f - Wy2));
+    sink.add(2, i2, j2 + 1, 1, Fz2 * (1.0f - Wx2) * Wy2);
+    sink.add(2, i2 + 1, j2 + 1, 1, Fz2 * Wx2 * Wy2);
+}
+
+// Left reflecting wall for one particle found behind it after the push
+// (particle_bc_user, user_pu/user_shock_pu.F90:557-602): trace back to the
+// crossing, deposit the path up to the wall, reflect with the wall's kick,
+// move on for the rest of the step, and cancel the behind-the-wall path the
+// deposit will add. Returns false when the particle cannot have crossed
+// this step (the reference removes it).
+template <class Sink>
+__device__ __forceinline__ bool wall_reflect(Sink &sink, float c, float gammawall, float betawall, double walloc,
+                                             long long mxcum, float q, float &x, float &y, float &z, float &u,
+                                             float v, float w) {
+    float gamma = sqrtf(1.0f + (u * u + v * v + w * w));
+    const float x0 = x - u / gamma * c;
+    const float y0 = y, z0 = z;
+    const double walloc0 = walloc - (double)(betawall * c) - (double)mxcum;
+    float tfrac = (float)fabs(((double)x0 - walloc0) / (double)(betawall * c - u / gamma * c));
+    if (!(tfrac < 1.0f)) return false;
+    const float xcolis = x0 + u / gamma * c * tfrac;
+    zigzag(sink, xcolis, y0, z0, x0, y0, z0, q);
+    u = gammawall * gammawall * gamma * (2.0f * betawall - u / gamma * (1.0f + betawall * betawall));
+    gamma = sqrtf(1.0f + (u * u + v * v + w * w));
+    tfrac = fminf(fabsf((x - xcolis) / fmaxf(fabsf(x - x0), 1e-9f)), 1.0f);
+    x = xcolis + u / gamma * c * tfrac;
+    y = y0;
+    z = z0;
+    zigzag(sink, xcolis, y0, z0, x - u / gamma * c, y - v / gamma * c, z - w / gamma * c, -q);
+    return true;
+}
 
 // ---------------------------------------------------------------------------
 // Esirkepov current of one particle moving x1 -> x2
@@ -466,6 +533,9 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
         for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
         __syncthreads();
     }
+    // shock hooks: wall position and the moving open boundary of this lap
+    const double walloc = (a.shock && a.wall) ? a.shock->walloc : -1.0e300;
+    const double x2in = a.shock ? a.shock->x2in : a.P.x2in;
     // particles since the last flush; the window is exact for up to 65536
     // contributions per cell, i.e. 65536 particles (every bound is uniform
     // across the CTA, so the barriers below are reached by all threads)
@@ -492,6 +562,12 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                         continue;
                     }
                     push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
+                    if (DIM == 2 && DEPOSIT && (double)(x + (float)a.P.mxcum) < walloc &&
+                        !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
+                                      y, z, u, v, w)) {
+                        sp.cell[n] = -1;  // removed by the wall (dropped by the next sort)
+                        continue;
+                    }
                 }
                 bool keep = true;
                 if (DEPOSIT) {
@@ -504,7 +580,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                     const float z0 = z - w * invgam * c;
                     const float q = sp.ch[n] * qs;
                     esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
-                    keep = wrap_particle<DIM>(g, a.P, x, y, z);
+                    keep = wrap_particle<DIM>(g, a.P, x, y, z, x2in);
                 }
                 int i, j, k;
                 const bool fin = isfinite(x) && isfinite(y) && isfinite(z);

@@ -60,6 +60,35 @@ class tg_config(ctypes.Structure):
     ]
 
 
+class tg_shock(ctypes.Structure):
+    _fields_ = [
+        ("wall", ctypes.c_int32), ("walloc", ctypes.c_double),
+        ("gammawall", ctypes.c_float), ("betawall", ctypes.c_float),
+        ("cond_i1", ctypes.c_int32), ("cond_i2", ctypes.c_int32),
+        ("edge_i1", ctypes.c_int32), ("edge_i2", ctypes.c_int32),
+        ("edge", ctypes.c_float * 6),
+        ("inject", ctypes.c_int32), ("xinject2", ctypes.c_double), ("betainj", ctypes.c_float),
+        ("xinj_max", ctypes.c_double),
+        ("ppc0", ctypes.c_float), ("gamma_drift", ctypes.c_float), ("weight", ctypes.c_float),
+        ("y1", ctypes.c_float), ("y2", ctypes.c_float),
+        ("delgam_i", ctypes.c_float), ("delgam_e", ctypes.c_float),
+        ("pcosthmult", ctypes.c_float), ("sigma_nonzero", ctypes.c_int32),
+        ("dseed", ctypes.c_double), ("totalpartnum", ctypes.c_int32),
+    ]
+
+
+def make_tg_shock(sh: dict) -> tg_shock:
+    """tg_shock from the dict of setups.shock_params"""
+    k = tg_shock()
+    for name, _ in tg_shock._fields_:
+        if name == "edge":
+            for a in range(6):
+                k.edge[a] = float(sh["edge"][a])
+        else:
+            setattr(k, name, sh[name])
+    return k
+
+
 class tg_diag(ctypes.Structure):
     _fields_ = [
         ("gauss_residual", ctypes.c_double), ("gauss_abs", ctypes.c_double),
@@ -82,6 +111,7 @@ ENTRY_POINTS = (
     "tg_ens_init", "tg_ens_finalize", "tg_ens_last_error", "tg_ens_bind_fields", "tg_ens_bind_particles",
     "tg_ens_sync_from_host", "tg_ens_sync_to_host", "tg_ens_step", "tg_ens_step_timed", "tg_ens_diag_fp64",
     "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
+    "tg_shock_init", "tg_shock_get", "tg_inject_region", "tg_particle_bc", "tg_field_bc", "tg_inject",
 )
 PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
@@ -137,6 +167,16 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_enable_timing.restype = ctypes.c_int
     lib.tg_phase_times.argtypes = [P, ctypes.c_void_p, ctypes.c_int32]
     lib.tg_phase_times.restype = ctypes.c_int
+    # collisionless-shock hooks
+    lib.tg_shock_init.argtypes = [P, ctypes.POINTER(tg_shock)]
+    lib.tg_shock_init.restype = ctypes.c_int
+    lib.tg_shock_get.argtypes = [P, ctypes.POINTER(tg_shock)]
+    lib.tg_shock_get.restype = ctypes.c_int
+    lib.tg_inject_region.argtypes = [P] + [ctypes.c_float] * 6
+    lib.tg_inject_region.restype = ctypes.c_int
+    for n in ("tg_particle_bc", "tg_field_bc", "tg_inject"):
+        getattr(lib, n).argtypes = [P]
+        getattr(lib, n).restype = ctypes.c_int
     # batched ensemble
     lib.tg_ens_init.argtypes = [ctypes.POINTER(tg_config), ctypes.c_int32, ctypes.POINTER(P)]
     lib.tg_ens_init.restype = ctypes.c_int
@@ -420,6 +460,28 @@ class GpuSim:
     def field(self, name: str) -> np.ndarray:
         c = self.cfg
         return self.fields[name].reshape(c.mz, c.my, c.mx)
+
+    # -- collisionless-shock hooks -------------------------------------------
+    def shock_init(self, sh: dict):
+        self._shock = make_tg_shock(sh)
+        self._check(self.lib.tg_shock_init(self.h, ctypes.byref(self._shock)))
+
+    def shock_state(self) -> dict:
+        k = tg_shock()
+        self._check(self.lib.tg_shock_get(self.h, ctypes.byref(k)))
+        return {n: (list(k.edge) if n == "edge" else getattr(k, n)) for n, _ in tg_shock._fields_}
+
+    def inject_region(self, x1, x2, y1, y2, ppc, weight=1.0):
+        self._check(self.lib.tg_inject_region(self.h, x1, x2, y1, y2, ppc, weight))
+
+    def particle_bc_user(self):
+        self._check(self.lib.tg_particle_bc(self.h))
+
+    def field_bc_user(self):
+        self._check(self.lib.tg_field_bc(self.h))
+
+    def inject_particles_user(self):
+        self._check(self.lib.tg_inject(self.h))
 
 
 def _diag_dict(d: tg_diag) -> dict:

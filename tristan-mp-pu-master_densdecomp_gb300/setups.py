@@ -48,6 +48,12 @@ WORKLOADS = {
     # data: still above L2) for kernel profiling
     "twostream2d_512_o3": dict(dims=2, order=3, nx=512, ny=512, c=0.45, c_omp=10.0,
                                ppc0=32.0, gamma0=0.5, delgam=0.005, ntimes=4),
+    # 2D pair shock: 8192 x 512, order 3, 16 ppc/species (ppc0 = 32),
+    # gamma0 = 15, kT = 1e-4, sigma = 0.1, open x, reflecting wall, moving
+    # injector (shock_params)
+    "shock2d_8192x512_o3": dict(dims=2, order=3, nx=8192, ny=512, c=0.45, c_omp=10.0, ppc0=32.0,
+                                gamma0=15.0, delgam=1e-4, sigma=0.1, ntimes=4, corr=1.0,
+                                periodic=(0, 1, 1)),
     # 3D Weibel: 256^3, order 2, 4 ppc/species, gamma0 = 5
     "weibel3d_256_o2": dict(dims=3, order=2, nx=256, ny=256, nz=256, c=0.45, c_omp=8.0,
                             ppc0=8.0, gamma0=5.0, delgam=0.01, ntimes=4),
@@ -158,3 +164,71 @@ def load_ensemble(cfgs, seed: int = 123457):
         with_capacity(cfg, len(ions), len(lecs))
         out.append((ions, lecs))
     return out
+
+
+def shock_params(cfg: SimConfig, betainj: float = 0.99999, leftwall: float = 20.0, btheta: float = 90.0,
+                 bphi: float = 0.0, wallgam: float = 1.0, temperature_ratio: float = 1.0,
+                 dseed: float = 123457.0):
+    """Hooks and initial fields of the collisionless-shock setup
+    (user_pu/user_shock_pu.F90 with wall = 1, rightclean = 0,
+    rightwall = 0), evaluated in single precision in the reference's order:
+    read_input_user (:118-186: wallgam, betainj, pcosthmult), init_EMfields
+    (:224-262: Binit, B along (btheta, bphi), E = -v x B of the upstream
+    flow), init_particle_distribution_user (:271-330: wall and injector
+    positions, x1in = 3, x2in = mx0 - 2), field_bc_user (:460-488).
+    Sets cfg.window; returns (hooks dict, initial fields dict, initial-load
+    region (x1, x2, y1, y2, ppc, weight))."""
+    f32 = np.float32
+    c = f32(cfg.c)
+    g0 = f32(cfg.gamma0)
+    if g0 < 1:
+        g0 = f32(np.sqrt(f32(1.0) / (f32(1.0) - g0 * g0)))
+    beta = f32(np.sqrt(f32(1.0) - f32(1.0) / (g0 * g0)))
+    qi = f32(cfg.qi)
+    me = f32(cfg.me) * abs(qi)
+    mi = f32(cfg.mi) * abs(qi)
+    ppc0 = f32(cfg.ppc0)
+    binit = f32(np.sqrt(f32(f32(f32(f32(g0 * ppc0) * f32(0.5)) * f32(c * c)) * f32(me * f32(f32(1.0) + me / mi)))
+                        * f32(cfg.sigma)))
+    pi_d = float(np.float32(3.1415927))
+    bth = f32(float(f32(btheta) / f32(180.0)) * pi_d)
+    bph = f32(float(f32(bphi) / f32(180.0)) * pi_d)
+    cos_t, sin_t = f32(np.cos(float(bth))), f32(np.sin(float(bth)))
+    cos_p, sin_p = f32(np.cos(float(bph))), f32(np.sin(float(bph)))
+    bx0 = f32(binit * cos_t)
+    by0 = f32(f32(binit * sin_t) * sin_p)
+    bz0 = f32(f32(binit * sin_t) * cos_p)
+    ex0 = f32(0.0)
+    ey0 = f32((-beta) * bz0)
+    ez0 = f32(-((-beta) * by0))
+    wg = f32(wallgam)
+    if wg == 0:
+        wg = f32(1.0)
+    if wg < 1:
+        wg = f32(np.copysign(f32(1.0) / np.sqrt(f32(1.0) - wg * wg), wg))
+    betawall = f32(np.sqrt(f32(1.0) - f32(1.0) / (wg * wg)))
+    mx, my = cfg.mx, cfg.my
+    xinject2 = float(f32(f32(mx - 2.0) / f32(2.0)))
+    delgam_i = f32(cfg.delgam)
+    delgam_e = f32(f32(f32(delgam_i * mi) / me) * f32(temperature_ratio))
+    sh = dict(wall=1, walloc=float(leftwall), gammawall=float(wg), betawall=float(betawall),
+              cond_i1=1, cond_i2=int(leftwall - 5.0), edge_i1=mx - 2, edge_i2=mx,
+              edge=[float(v) for v in (ex0, ey0, ez0, bx0, by0, bz0)],
+              inject=1, xinject2=xinject2, betainj=float(f32(betainj)), xinj_max=float(mx - 15),
+              ppc0=float(ppc0), gamma_drift=float(-g0), weight=1.0, y1=3.0, y2=float(my - 2.0),
+              delgam_i=float(delgam_i), delgam_e=float(delgam_e),
+              pcosthmult=1.0 if binit != 0 else 0.0, sigma_nonzero=int(cfg.sigma != 0),
+              dseed=float(dseed), totalpartnum=0)
+    n = cfg.ncells
+    fields = {k: np.full(n, v, np.float32) for k, v in
+              (("ex", ex0), ("ey", ey0), ("ez", ez0), ("bx", bx0), ("by", by0), ("bz", bz0))}
+    cfg.window = (3.0, float(mx - 2.0)) + tuple(cfg.window_in()[2:]) if cfg.window is None else cfg.window
+    region = (float(f32(leftwall)), float(f32(xinject2)), 3.0, float(my - 2.0), float(ppc0), 1.0)
+    return sh, fields, region
+
+
+def shock_capacity(cfg: SimConfig, laps: int, sh: dict) -> int:
+    """particles per species after the initial load and `laps` injections"""
+    per_lap = 0.5 * cfg.ppc0 * (cfg.my - cfg.nghost) * (1.0 + sh["betainj"]) * cfg.c
+    init = 0.5 * cfg.ppc0 * (cfg.my - cfg.nghost) * (sh["xinject2"] - 20.0)
+    return int(init + per_lap * (laps + 2)) + 4096
