@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--sort-every", type=int, default=0, help="0: chosen by the autotuner")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-shock", action="store_true")
+    ap.add_argument("--shock-steps", type=int, default=100)
     ap.add_argument("--ens-boxes", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=40)
     ap.add_argument("--ens-tile", type=int, nargs=2, default=None,
@@ -322,10 +324,56 @@ def run_ensemble(args, device):
     }
 
 
+def run_shock(args, device):
+    """The 2D pair shock on 8192 x 512 cells (order 3, 16 per cell per
+    species upstream, gamma0 = 15, sigma = 0.1): the initial half-box load
+    drawn on the device, then laps with the reflecting wall, conductor and
+    moving injector running as kernels inside the lap (graph-replayed, tile
+    sort every lap). particle-steps/s use the mean particle count of the
+    timed laps."""
+    from tristan_gb300 import setups
+    from tristan_gb300.gpu import GpuSim, SYNC_ALL
+    cfg = setups.make_config("shock2d_8192x512_o3", sort_every=1)
+    sh, fields, region = setups.shock_params(cfg)
+    K = max(2, args.shock_steps // 2 * 2)
+    warm = max(args.warmup, 4) // 2 * 2
+    cfg.maxhlf = setups.shock_capacity(cfg, K + warm, sh)
+    g = GpuSim(cfg, device=device)
+    g.set_fields(**fields)
+    g.sync_from_host(SYNC_ALL)
+    g.shock_init(sh)
+    t0 = time.perf_counter()
+    g.inject_region(*region)
+    g.synchronize()
+    t_load = time.perf_counter() - t0
+    n_load = sum(g.counts())
+    g.step(warm)
+    g.synchronize()
+    n0 = sum(g.counts())
+    ms = g.step_timed(K)
+    n1 = sum(g.counts())
+    st = g.shock_state()
+    kps = g.kernels_per_step()
+    g.close()
+    mean_n = 0.5 * (n0 + n1)
+    return {"workload": "shock2d_8192x512_o3", "grid": [cfg.nx, cfg.ny], "order": cfg.order,
+            "ppc_per_species_upstream": int(cfg.ppc0 // 2), "steps": K, "warmup": warm,
+            "value": mean_n * K / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / K,
+            "particles_initial_load": n_load, "particles_timed": [n0, n1],
+            "device_load_s": t_load, "xinject2": st["xinject2"], "walloc": st["walloc"],
+            "kernels_per_step": kps, "deposit": "fp32-atomic", "sort_every": 1,
+            "hooks": "reflecting wall + zigzag, conductor, moving injector (jump-ahead Park-Miller)"}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup(args)
     pkg = __graft_entry__.load_package()
+    if args.workload == "shock2d_8192x512_o3":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": args.workload,
+                              "shock": run_shock(args, local)}), flush=True)
+        return
     if args.workload == "ensemble64":
         # the ensemble alone (its numbers also ride on the default line)
         if rank == 0:
@@ -409,6 +457,9 @@ def main():
     ens = None
     if rank == 0 and not args.no_ensemble:
         ens = run_ensemble(args, device)
+    shock = None
+    if rank == 0 and not args.no_shock:
+        shock = run_shock(args, device)
     if rank != 0:
         return
     d = hist[-1] if len(hist) else None
@@ -417,7 +468,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config, "fixed_point": fixed, "phase_ms_per_lap": phases,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": kps * args.steps, "ensemble": ens,
+            "gpu_launches": kps * args.steps, "ensemble": ens, "shock": shock,
             "gauss_residual_last_lap": (float(np.sqrt(d[0] / d[1])) if d is not None and d[1] > 0 else None)}
     print(json.dumps(line), flush=True)
 

@@ -154,9 +154,11 @@ int tg_add_current(tg_ctx *ctx);
    lap after the previous reorder). force != 0 sorts now. */
 int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force);
 
-/* One or more complete laps of the periodic main loop
-   (code/tristanmainloop.F90:115-303 without output, injection and domain
-   moves), fused and replayed from a captured CUDA graph. */
+/* One or more complete laps of the main loop
+   (code/tristanmainloop.F90:115-303 without output and domain moves; with
+   the shock hooks set, also particle_bc_user, field_bc_user and
+   inject_particles_user at their places), fused and replayed from a
+   captured CUDA graph. */
 int tg_step(tg_ctx *ctx, int32_t nsteps);
 /* tg_step bracketed by CUDA events on the context's stream; *ms receives
    the device time of the nsteps laps. Synchronises. */
@@ -270,6 +272,64 @@ int tg_inject_region(tg_ctx *ctx, float x1, float x2, float y1, float y2, float 
 int tg_particle_bc(tg_ctx *ctx);
 int tg_field_bc(tg_ctx *ctx);
 int tg_inject(tg_ctx *ctx);
+
+/* ---------------------------------------------------------------------
+   Restart files in the reference's format: the fields file of
+   write_restart (code/output.F90:2192-2201: one unformatted record of
+   mx, my, mz, ex, ey, ez, bx, by, bz, dseed, lap, xinject, xinject2,
+   xinject3, leftwall, walloc) and its particle file (:2202-2218: ions,
+   lecs, maxptl, maxhlf, totalpartnum, then x of the ions and of the
+   electrons, y, z, u, v, w, ch, ind, proc, splitlev), read back as
+   restart() does (code/restart.F90:209-255). Records follow gfortran's
+   unformatted sequential layout (4-byte signed markers, subrecords of at
+   most 2147483639 bytes).
+   --------------------------------------------------------------------- */
+typedef struct {
+    double dseed;
+    int32_t lap;
+    double xinject, xinject2, xinject3;
+    float leftwall;
+    double walloc;
+    int32_t totalpartnum;
+    int32_t maxptl;           /* written as is (0: 2 maxhlf) */
+    int64_t max_subrecord;    /* 0: gfortran's 2147483639 bytes */
+} tg_restart_meta;
+/* Write the device state (synchronises). With the shock hooks set, dseed,
+   xinject2, walloc and totalpartnum come from the device. */
+int tg_write_restart(tg_ctx *ctx, const char *fields_path, const char *particles_path,
+                     const tg_restart_meta *meta);
+/* Load a restart into the context (the grid must match); *out receives the
+   scalars (the shock hooks, when set, take dseed, xinject2, walloc and
+   totalpartnum). Currents are not part of the files. */
+int tg_read_restart(tg_ctx *ctx, const char *fields_path, const char *particles_path, tg_restart_meta *out);
+
+/* Grid moments of the particles for output_tot (meanq_fld_cur,
+   code/output.F90:5222-5482): each particle adds its quantity and its
+   weight to the cells of the box (i +- idx, j +- idy, k +- idz) around its
+   cell (2D: idz ignored); ghost layers are folded as exchange_current does,
+   each cell is divided by its box size, and the velocity-like moments by
+   the summed weight. kind: TG_MOMENT_* below, the reference's names.
+   num and den are host arrays of mx*my*mz floats. Sums are FP64, rounded to
+   single once (the reference sums in single, particle by particle), so
+   densities of unit weights are exact. Synchronises. */
+#define TG_MOMENT_TDENS 0
+#define TG_MOMENT_IDENS 1
+#define TG_MOMENT_TBETX 2
+#define TG_MOMENT_TBETY 3
+#define TG_MOMENT_TBETZ 4
+#define TG_MOMENT_IBETX 5
+#define TG_MOMENT_IBETY 6
+#define TG_MOMENT_IBETZ 7
+#define TG_MOMENT_TMOMX 8
+#define TG_MOMENT_TMOMY 9
+#define TG_MOMENT_TMOMZ 10
+#define TG_MOMENT_IMOMX 11
+#define TG_MOMENT_IMOMY 12
+#define TG_MOMENT_IMOMZ 13
+#define TG_MOMENT_EENER 14
+#define TG_MOMENT_IENER 15
+#define TG_MOMENT_KINDS 16
+int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz, float *num, float *den);
 
 /* ---------------------------------------------------------------------
    Batched ensemble: many independent periodic 2D boxes of uneven size

@@ -148,6 +148,9 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_charge_density.restype = None
             lib.to_num_threads.argtypes = []
             lib.to_num_threads.restype = ctypes.c_int
+            lib.to_meanq.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p]
+            lib.to_meanq.restype = None
             K = ctypes.POINTER(to_shock)
             lib.to_random.argtypes = [ctypes.POINTER(ctypes.c_double)]
             lib.to_random.restype = ctypes.c_float
@@ -287,6 +290,13 @@ class OracleSim:
 
     def shock_call(self, name: str) -> None:
         getattr(self.lib, name)(self.ptr, self.kptr)
+
+    def meanq(self, kind: int, idx: int = 2, idy: int = 2, idz: int = 2):
+        num = np.zeros(self.lot, np.float32)
+        den = np.zeros(self.lot, np.float32)
+        self.lib.to_meanq(self.ptr, kind, idx, idy, idz if self.cfg.dims == 3 else 0, num.ctypes.data,
+                          den.ctypes.data)
+        return num, den
 
     def charge_density(self) -> np.ndarray:
         rho = np.zeros(self.lot, np.float64)

@@ -1503,3 +1503,86 @@ void to_step_shock(to_state *s, to_shock *k)
     to_reorder_particles(s);
     s->lap++;
 }
+
+/* ------------------------------------------------------------------------
+ * Grid moments of the particles (meanq_fld_cur, code/output.F90:5222-5482):
+ * every particle adds its quantity (and its weight) to the cells of a
+ * (2 idx + 1) x (2 idy + 1) [x (2 idz + 1)] box around its cell, the ghost
+ * layers are folded (exchange_current), each cell is divided by its box
+ * size, and for the velocity-like moments by the summed weight.
+ * --------------------------------------------------------------------- */
+void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, float *den)
+{
+    const int64_t lot = to_lot(s);
+    float *cx = s->curx, *cy = s->cury, *cz = s->curz;
+    /* the reference computes into the current arrays: keep them */
+    float *keep = malloc(sizeof(float) * 3 * lot);
+    memcpy(keep, cx, sizeof(float) * lot);
+    memcpy(keep + lot, cy, sizeof(float) * lot);
+    memcpy(keep + 2 * lot, cz, sizeof(float) * lot);
+    memset(cx, 0, sizeof(float) * lot);
+    memset(cy, 0, sizeof(float) * lot);
+    memset(cz, 0, sizeof(float) * lot);
+    const int64_t iy = s->mx, iz = (int64_t)s->mx * s->my;
+    for (int sp = 0; sp < 2; sp++) {
+        const int64_t base = sp == 0 ? 0 : s->maxhlf, cnt = sp == 0 ? s->ions : s->lecs;
+        for (int64_t n = 0; n < cnt; n++) {
+            const to_particle *p = &s->p[base + n];
+            const float gamprt = 1.0f / sqrtf(1.0f + p->u * p->u + p->v * p->v + p->w * p->w);
+            float ax = 0.0f, ay = 0.0f;
+            const int ion = sp == 0, lec = sp == 1;
+            switch (kind) {
+            case 0: ax = p->ch; break;                                              /* tdens */
+            case 1: if (ion) ax = p->ch; break;                                     /* idens */
+            case 2: ax = p->u * gamprt * p->ch; ay = p->ch; break;                  /* tbetx */
+            case 3: ax = p->v * gamprt * p->ch; ay = p->ch; break;                  /* tbety */
+            case 4: ax = p->w * gamprt * p->ch; ay = p->ch; break;                  /* tbetz */
+            case 5: if (ion) { ax = p->u * gamprt * p->ch; ay = p->ch; } break;     /* ibetx */
+            case 6: if (ion) { ax = p->v * gamprt * p->ch; ay = p->ch; } break;     /* ibety */
+            case 7: if (ion) { ax = p->w * gamprt * p->ch; ay = p->ch; } break;     /* ibetz */
+            case 8: ax = p->u * p->ch; ay = p->ch; break;                           /* tmomx */
+            case 9: ax = p->v * p->ch; ay = p->ch; break;                           /* tmomy */
+            case 10: ax = p->w * p->ch; ay = p->ch; break;                          /* tmomz */
+            case 11: if (ion) { ax = p->u * p->ch; ay = p->ch; } break;             /* imomx */
+            case 12: if (ion) { ax = p->v * p->ch; ay = p->ch; } break;             /* imomy */
+            case 13: if (ion) { ax = p->w * p->ch; ay = p->ch; } break;             /* imomz */
+            case 14: if (lec) { ax = (1.0f / gamprt - 1.0f) * p->ch; ay = p->ch; } break; /* eener */
+            case 15: if (ion) { ax = (1.0f / gamprt - 1.0f) * p->ch; ay = p->ch; } break; /* iener */
+            default: break;
+            }
+            const int i = (int)p->x, j = (int)p->y, k = (int)p->z;
+            int lz1 = k - idz > 1 ? k - idz : 1, lz2 = k + idz < s->mz ? k + idz : s->mz;
+            if (s->dims == 2) { lz1 = 1; lz2 = 1; }
+            const int ly1 = j - idy > 1 ? j - idy : 1, ly2 = j + idy < s->my ? j + idy : s->my;
+            const int lx1 = i - idx > 1 ? i - idx : 1, lx2 = i + idx < s->mx ? i + idx : s->mx;
+            for (int kk = lz1; kk <= lz2; kk++)
+                for (int jj = ly1; jj <= ly2; jj++)
+                    for (int ii = lx1; ii <= lx2; ii++) {
+                        const int64_t l = (ii - 1) + iy * (jj - 1) + iz * (kk - 1);
+                        cx[l] = cx[l] + ax;
+                        cy[l] = cy[l] + ay;
+                    }
+        }
+    }
+    to_exchange_current(s);
+    for (int k = 1; k <= s->mz; k++)
+        for (int j = 1; j <= s->my; j++)
+            for (int i = 1; i <= s->mx; i++) {
+                int lz1 = k - idz > 1 ? k - idz : 1, lz2 = k + idz < s->mz ? k + idz : s->mz;
+                if (s->dims == 2) { lz1 = 1; lz2 = 1; }
+                const int ly1 = j - idy > 1 ? j - idy : 1, ly2 = j + idy < s->my ? j + idy : s->my;
+                const int lx1 = i - idx > 1 ? i - idx : 1, lx2 = i + idx < s->mx ? i + idx : s->mx;
+                const int64_t l = (i - 1) + iy * (j - 1) + iz * (k - 1);
+                const float box = (float)((lx2 - lx1 + 1) * (ly2 - ly1 + 1) * (lz2 - lz1 + 1));
+                cx[l] = cx[l] / box;
+                cy[l] = cy[l] / box;
+            }
+    if (kind >= 2)
+        for (int64_t l = 0; l < lot; l++) cx[l] = cy[l] != 0.0f ? cx[l] / cy[l] : 0.0f;
+    memcpy(num, cx, sizeof(float) * lot);
+    memcpy(den, cy, sizeof(float) * lot);
+    memcpy(cx, keep, sizeof(float) * lot);
+    memcpy(cy, keep + lot, sizeof(float) * lot);
+    memcpy(cz, keep + 2 * lot, sizeof(float) * lot);
+    free(keep);
+}

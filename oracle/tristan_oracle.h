@@ -201,6 +201,11 @@ void to_field_bc_user(to_state *s, const to_shock *k);            /* :460-488 */
 /* the shock's lap: the periodic lap with the user hooks at their places
    in code/tristanmainloop.F90:117-303 */
 void to_step_shock(to_state *s, to_shock *k);
+/* grid moments of meanq_fld_cur (code/output.F90:5222-5482); kind 0..15 =
+   tdens idens tbetx tbety tbetz ibetx ibety ibetz tmomx tmomy tmomz imomx
+   imomy imomz eener iener; num receives the moment, den the box-averaged
+   weight (both mx*my*mz); the current arrays are left as they were */
+void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, float *den);
 /* sin and cos of a float argument, evaluated in double and rounded once */
 void to_sincosf(float x, float *sn, float *cs);
 

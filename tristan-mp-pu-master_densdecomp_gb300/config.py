@@ -148,3 +148,57 @@ class SimConfig:
         else:
             minz, maxz = float(ngz // 2 + 1), float(ngz // 2 + 1) + 1.0
         return (minx, maxx), (miny, maxy), (minz, maxz)
+
+
+def parse_input(path: str) -> dict:
+    """The reference's `input` file as {section: {key: value}}: sections are
+    `<name>` lines, entries `key = value`, `#` starts a comment (the format
+    read by code/inputparser.c / code/inputparserf.F90); values parse as int
+    or float where they can."""
+    out: dict = {}
+    sec = ""
+    with open(path) as fh:
+        for raw in fh:
+            line = raw.split("#", 1)[0].strip()
+            if not line:
+                continue
+            if line.startswith("<") and line.endswith(">"):
+                sec = line[1:-1].strip()
+                out.setdefault(sec, {})
+                continue
+            if "=" not in line:
+                continue
+            k, v = (t.strip() for t in line.split("=", 1))
+            for conv in (int, float):
+                try:
+                    v = conv(v)
+                    break
+                except ValueError:
+                    continue
+            out.setdefault(sec, {})[k] = v
+    return out
+
+
+def from_input(path: str, dims: int, order: int, **overrides) -> SimConfig:
+    """SimConfig from a reference `input` file. dims and order are the
+    reference's compile-time choices (-DtwoD, -Ddd1/2/3); the keys used are
+    those of read_input_grid, read_input_particles, read_input_algorithm and
+    read_input_boundaries with the reference's defaults where absent
+    (code/fields.F90:154-192, code/particles.F90:189-233,
+    code/initialize.F90:293-305)."""
+    d = parse_input(path)
+    get = lambda sec, key, default: d.get(sec, {}).get(key, default)
+    kw = dict(dims=dims, order=order,
+              nx=int(get("grid", "mx0", 128)), ny=int(get("grid", "my0", 128)),
+              nz=int(get("grid", "mz0", 1)) if dims == 3 else 1,
+              c=float(get("time", "c", 0.45)),
+              corr=float(get("algorithm", "Corr", 1.025)), ntimes=int(get("algorithm", "ntimes", 4)),
+              ppc0=float(get("particles", "ppc0", 16)), gamma0=float(get("particles", "gamma0", 1.0)),
+              delgam=float(get("particles", "delgam", 1e-4)), me=float(get("particles", "me", 1.0)),
+              mi=float(get("particles", "mi", 1.0)), c_omp=float(get("particles", "c_omp", 10.0)),
+              sigma=float(get("particles", "sigma", 0.0)),
+              periodic=(int(get("boundaries", "periodicx", 1)), int(get("boundaries", "periodicy", 1)),
+                        int(get("boundaries", "periodicz", 1))),
+              external_fields=int(get("problem", "external_fields", 0)))
+    kw.update(overrides)
+    return SimConfig(**kw)

@@ -73,6 +73,8 @@ struct tg_ctx {
     ShockState *d_shock = nullptr;
     float *d_tables = nullptr;  // gt_i, pt_i, gt_e, pt_e
     tg_shock hshock;
+    // grid-moment scratch (FP64 sums)
+    double *mom[2] = {};
     char err[512] = {0};
     std::vector<void *> allocs;
 };
@@ -440,6 +442,25 @@ extern "C" int tg_bind_particles(tg_ctx *ctx, void *p, int32_t *ions, int32_t *l
 
 static const size_t AOS = 40;
 
+// A device-usable view of a host array: the device pointer of page-locked
+// (registered) memory, or the pointer itself when the device reads pageable
+// host memory coherently (NVLink-C2C systems); NULL otherwise (staged
+// copies are used then).
+static void *host_view(tg_ctx *ctx, void *h) {
+    if ((uintptr_t)h & 7) return nullptr;  // the conversion kernels move 8-byte words
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, h) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+        return at.devicePointer;
+    (void)cudaGetLastError();
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) ==
+            cudaSuccess &&
+        pageable)
+        return h;
+    (void)cudaGetLastError();
+    return nullptr;
+}
+
 extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
     if (!ctx) return TG_ERR_ARG;
     const size_t lot = (size_t)ctx->g.lot;
@@ -459,11 +480,18 @@ extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
             if (n[s] < 0 || n[s] > ctx->cfg.maxhlf)
                 return fail(ctx, TG_ERR_OVERFLOW, "species %d count %lld outside [0, maxhlf=%lld]", s, n[s],
                             (long long)ctx->cfg.maxhlf);
-        if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+        const char *hbase = (const char *)host_view(ctx, ctx->hp);
+        if (!hbase && !ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
         for (int s = 0; s < 2; s++) {
-            const char *src = (const char *)ctx->hp + (s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS);
-            CK(cudaMemcpyAsync(ctx->stage, src, (size_t)n[s] * AOS, cudaMemcpyHostToDevice, ctx->st));
-            CK(launch_aos_to_soa(ctx->g, ctx->stage, ctx->sp[ctx->par][s], n[s], ctx->d_status, ctx->st));
+            const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+            if (hbase) {
+                // the conversion kernel reads the host records directly
+                CK(launch_aos_to_soa(ctx->g, hbase + off, ctx->sp[ctx->par][s], n[s], ctx->d_status, ctx->st));
+            } else {
+                const char *src = (const char *)ctx->hp + off;
+                CK(cudaMemcpyAsync(ctx->stage, src, (size_t)n[s] * AOS, cudaMemcpyHostToDevice, ctx->st));
+                CK(launch_aos_to_soa(ctx->g, ctx->stage, ctx->sp[ctx->par][s], n[s], ctx->d_status, ctx->st));
+            }
             CK(cudaMemcpyAsync(ctx->d_cnt + 2 * ctx->par + s, &n[s], sizeof(long long), cudaMemcpyHostToDevice,
                                ctx->st));
             ctx->hcount[s] = n[s];
@@ -516,12 +544,19 @@ extern "C" int tg_sync_to_host(tg_ctx *ctx, unsigned mask) {
         long long n[2];
         int r = exact_counts(ctx, n);
         if (r) return r;
-        if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+        char *hbase = (char *)host_view(ctx, ctx->hp);
+        if (!hbase && !ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
         for (int s = 0; s < 2; s++) {
-            char *dst = (char *)ctx->hp + (s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS);
-            CK(launch_soa_to_aos(ctx->g, ctx->sp[ctx->par][s], ctx->stage, n[s], ctx->st));
-            CK(cudaMemcpyAsync(dst, ctx->stage, (size_t)n[s] * AOS, cudaMemcpyDeviceToHost, ctx->st));
-            CK(cudaStreamSynchronize(ctx->st));
+            const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+            if (hbase) {
+                // the conversion kernel writes the host records directly
+                CK(launch_soa_to_aos(ctx->g, ctx->sp[ctx->par][s], hbase + off, n[s], ctx->st));
+            } else {
+                char *dst = (char *)ctx->hp + off;
+                CK(launch_soa_to_aos(ctx->g, ctx->sp[ctx->par][s], ctx->stage, n[s], ctx->st));
+                CK(cudaMemcpyAsync(dst, ctx->stage, (size_t)n[s] * AOS, cudaMemcpyDeviceToHost, ctx->st));
+                CK(cudaStreamSynchronize(ctx->st));
+            }
         }
         *ctx->hions = (int32_t)n[0];
         *ctx->hlecs = (int32_t)n[1];
@@ -1127,5 +1162,275 @@ extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
     double h[16];
     if (tg_diag_history(ctx, h, 1) != 1) return fail(ctx, TG_ERR_STATE, "tg_diag_fp64: no record");
     record_to_diag(h, out);
+    return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// restart files in the reference's format (write_restart,
+// code/output.F90:2192-2222; restart, code/restart.F90:209-255): one
+// gfortran unformatted sequential record per file, split into subrecords of
+// at most 2147483639 bytes whose signed 4-byte markers say whether the
+// record continues (leading marker < 0) or continues a previous subrecord
+// (trailing marker < 0)
+// ---------------------------------------------------------------------------
+namespace {
+const int64_t GFORTRAN_MAX_SUBRECORD = 2147483639LL;
+
+struct RecordWriter {
+    FILE *f = nullptr;
+    int64_t max_sub = GFORTRAN_MAX_SUBRECORD;
+    int64_t total = 0, written = 0, in_sub = 0, sub_len = 0;
+    bool first = true, ok = true;
+    void marker(int32_t m) { ok = ok && fwrite(&m, 4, 1, f) == 1; }
+    void open_sub() {
+        sub_len = std::min(max_sub, total - written);
+        const bool last = written + sub_len >= total;
+        marker(last ? (int32_t)sub_len : -(int32_t)sub_len);
+        in_sub = 0;
+    }
+    void close_sub() {
+        marker(first ? (int32_t)sub_len : -(int32_t)sub_len);
+        first = false;
+    }
+    void begin(int64_t bytes) {
+        total = bytes;
+        written = 0;
+        first = true;
+        open_sub();
+        if (total == 0) close_sub();
+    }
+    void put(const void *p, int64_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        while (n > 0 && ok) {
+            const int64_t k = std::min(n, sub_len - in_sub);
+            ok = ok && fwrite(c, 1, (size_t)k, f) == (size_t)k;
+            c += k;
+            n -= k;
+            in_sub += k;
+            written += k;
+            if (in_sub == sub_len) {
+                close_sub();
+                if (written < total) open_sub();
+            }
+        }
+    }
+};
+
+// one whole logical record
+bool read_record(FILE *f, std::vector<unsigned char> &out) {
+    out.clear();
+    bool first = true;
+    for (;;) {
+        int32_t lead = 0, tail = 0;
+        if (fread(&lead, 4, 1, f) != 1) return false;
+        const int64_t len = lead < 0 ? -(int64_t)lead : lead;
+        const size_t at = out.size();
+        out.resize(at + (size_t)len);
+        if (len > 0 && fread(out.data() + at, 1, (size_t)len, f) != (size_t)len) return false;
+        if (fread(&tail, 4, 1, f) != 1) return false;
+        const int64_t tlen = tail < 0 ? -(int64_t)tail : tail;
+        if (tlen != len || (tail < 0) == first) return false;
+        first = false;
+        if (lead >= 0) return true;
+    }
+}
+
+struct Cursor {
+    const unsigned char *p, *end;
+    template <class T>
+    bool get(T &v) {
+        if (end - p < (ptrdiff_t)sizeof(T)) return false;
+        memcpy(&v, p, sizeof(T));
+        p += sizeof(T);
+        return true;
+    }
+    bool take(void *dst, size_t n) {
+        if ((size_t)(end - p) < n) return false;
+        memcpy(dst, p, n);
+        p += n;
+        return true;
+    }
+};
+
+struct AosRec {
+    float x, y, z, u, v, w, ch;
+    int32_t ind, proc, splitlev;
+};
+}  // namespace
+
+extern "C" int tg_write_restart(tg_ctx *ctx, const char *fld_path, const char *prt_path,
+                                const tg_restart_meta *meta) {
+    if (!ctx || !fld_path || !prt_path || !meta) return TG_ERR_ARG;
+    tg_restart_meta m = *meta;
+    if (ctx->shock_on) {
+        ShockState S;
+        CK(cudaMemcpyAsync(&S, ctx->d_shock, sizeof S, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        m.dseed = (double)S.seed;
+        m.xinject2 = S.xinject2;
+        m.walloc = S.walloc;
+        m.totalpartnum = S.totalpartnum;
+    }
+    const int64_t max_sub = m.max_subrecord > 0 ? m.max_subrecord : GFORTRAN_MAX_SUBRECORD;
+    const size_t lot = (size_t)ctx->g.lot;
+    // fields
+    std::vector<float> fl(6 * lot);
+    for (int a = 0; a < 6; a++)
+        CK(cudaMemcpyAsync(fl.data() + a * lot, ctx->f[a], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    FILE *f = fopen(fld_path, "wb");
+    if (!f) return fail(ctx, TG_ERR_ARG, "tg_write_restart: cannot open %s", fld_path);
+    RecordWriter w;
+    w.f = f;
+    w.max_sub = max_sub;
+    const int32_t dims3[3] = {ctx->g.mx, ctx->g.my, ctx->g.mz};
+    w.begin(12 + 24 * (int64_t)lot + 8 + 4 + 24 + 4 + 8);
+    w.put(dims3, 12);
+    w.put(fl.data(), 24 * (int64_t)lot);
+    w.put(&m.dseed, 8);
+    w.put(&m.lap, 4);
+    w.put(&m.xinject, 8);
+    w.put(&m.xinject2, 8);
+    w.put(&m.xinject3, 8);
+    w.put(&m.leftwall, 4);
+    w.put(&m.walloc, 8);
+    const bool okf = w.ok && fclose(f) == 0;
+    if (!okf) return fail(ctx, TG_ERR_ARG, "tg_write_restart: write to %s failed", fld_path);
+    // particles
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+    std::vector<AosRec> pa[2];
+    for (int s = 0; s < 2; s++) {
+        pa[s].resize((size_t)n[s]);
+        if (n[s] == 0) continue;
+        CK(launch_soa_to_aos(ctx->g, ctx->sp[ctx->par][s], ctx->stage, n[s], ctx->st));
+        CK(cudaMemcpyAsync(pa[s].data(), ctx->stage, (size_t)n[s] * AOS, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    f = fopen(prt_path, "wb");
+    if (!f) return fail(ctx, TG_ERR_ARG, "tg_write_restart: cannot open %s", prt_path);
+    RecordWriter wp;
+    wp.f = f;
+    wp.max_sub = max_sub;
+    const int32_t head[5] = {(int32_t)n[0], (int32_t)n[1], m.maxptl > 0 ? m.maxptl : (int32_t)(2 * ctx->cfg.maxhlf),
+                             (int32_t)ctx->cfg.maxhlf, m.totalpartnum};
+    wp.begin(20 + 40 * (n[0] + n[1]));
+    wp.put(head, 20);
+    std::vector<char> col;
+    for (int comp = 0; comp < 10; comp++)
+        for (int s = 0; s < 2; s++) {
+            col.resize((size_t)n[s] * 4);
+            for (long long i = 0; i < n[s]; i++)
+                memcpy(col.data() + 4 * i, (const char *)&pa[s][(size_t)i] + 4 * comp, 4);
+            wp.put(col.data(), (int64_t)col.size());
+        }
+    const bool okp = wp.ok && fclose(f) == 0;
+    if (!okp) return fail(ctx, TG_ERR_ARG, "tg_write_restart: write to %s failed", prt_path);
+    return check_status(ctx);
+}
+
+extern "C" int tg_read_restart(tg_ctx *ctx, const char *fld_path, const char *prt_path, tg_restart_meta *out) {
+    if (!ctx || !fld_path || !prt_path || !out) return TG_ERR_ARG;
+    std::vector<unsigned char> rec;
+    FILE *f = fopen(fld_path, "rb");
+    if (!f) return fail(ctx, TG_ERR_ARG, "tg_read_restart: cannot open %s", fld_path);
+    const bool okr = read_record(f, rec);
+    fclose(f);
+    if (!okr) return fail(ctx, TG_ERR_ARG, "tg_read_restart: %s is not one unformatted record", fld_path);
+    const size_t lot = (size_t)ctx->g.lot;
+    Cursor c{rec.data(), rec.data() + rec.size()};
+    int32_t d3[3];
+    if (!c.take(d3, 12) || d3[0] != ctx->g.mx || d3[1] != ctx->g.my || d3[2] != ctx->g.mz)
+        return fail(ctx, TG_ERR_ARG, "tg_read_restart: grid %d x %d x %d does not match the context", d3[0], d3[1],
+                    d3[2]);
+    std::vector<float> fl(6 * lot);
+    tg_restart_meta m;
+    memset(&m, 0, sizeof m);
+    if (!c.take(fl.data(), 24 * lot) || !c.get(m.dseed) || !c.get(m.lap) || !c.get(m.xinject) ||
+        !c.get(m.xinject2) || !c.get(m.xinject3) || !c.get(m.leftwall) || !c.get(m.walloc))
+        return fail(ctx, TG_ERR_ARG, "tg_read_restart: %s is short", fld_path);
+    f = fopen(prt_path, "rb");
+    if (!f) return fail(ctx, TG_ERR_ARG, "tg_read_restart: cannot open %s", prt_path);
+    const bool okp = read_record(f, rec);
+    fclose(f);
+    if (!okp) return fail(ctx, TG_ERR_ARG, "tg_read_restart: %s is not one unformatted record", prt_path);
+    Cursor p{rec.data(), rec.data() + rec.size()};
+    int32_t head[5];
+    if (!p.take(head, 20)) return fail(ctx, TG_ERR_ARG, "tg_read_restart: %s is short", prt_path);
+    const long long n[2] = {head[0], head[1]};
+    for (int s = 0; s < 2; s++)
+        if (n[s] < 0 || n[s] > ctx->cfg.maxhlf)
+            return fail(ctx, TG_ERR_OVERFLOW, "tg_read_restart: species %d count %lld outside [0, maxhlf=%lld]", s,
+                        n[s], (long long)ctx->cfg.maxhlf);
+    if ((size_t)(p.end - p.p) < (size_t)(40 * (n[0] + n[1])))
+        return fail(ctx, TG_ERR_ARG, "tg_read_restart: %s is short", prt_path);
+    m.maxptl = head[2];
+    m.totalpartnum = head[4];
+    std::vector<AosRec> pa[2];
+    for (int s = 0; s < 2; s++) pa[s].resize((size_t)n[s]);
+    for (int comp = 0; comp < 10; comp++)
+        for (int s = 0; s < 2; s++)
+            for (long long i = 0; i < n[s]; i++) {
+                memcpy((char *)&pa[s][(size_t)i] + 4 * comp, p.p, 4);
+                p.p += 4;
+            }
+    // upload
+    for (int a = 0; a < 6; a++)
+        CK(cudaMemcpyAsync(ctx->f[a], fl.data() + a * lot, lot * 4, cudaMemcpyHostToDevice, ctx->st));
+    if (!ctx->stage) CK(cudaMalloc(&ctx->stage, (size_t)ctx->cfg.maxhlf * AOS + 256));
+    for (int s = 0; s < 2; s++) {
+        if (n[s] > 0) {
+            CK(cudaMemcpyAsync(ctx->stage, pa[s].data(), (size_t)n[s] * AOS, cudaMemcpyHostToDevice, ctx->st));
+            CK(launch_aos_to_soa(ctx->g, ctx->stage, ctx->sp[ctx->par][s], n[s], ctx->d_status, ctx->st));
+        }
+        CK(cudaMemcpyAsync(ctx->d_cnt + 2 * ctx->par + s, &n[s], sizeof(long long), cudaMemcpyHostToDevice,
+                           ctx->st));
+        ctx->hcount[s] = n[s];
+    }
+    if (ctx->shock_on) {
+        ShockState S;
+        CK(cudaMemcpyAsync(&S, ctx->d_shock, sizeof S, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        S.seed = (long long)m.dseed;
+        S.xinject2 = m.xinject2;
+        S.walloc = m.walloc;
+        S.totalpartnum = m.totalpartnum;
+        if (ctx->K.inject) S.x2in = m.xinject2;
+        CK(cudaMemcpyAsync(ctx->d_shock, &S, sizeof S, cudaMemcpyHostToDevice, ctx->st));
+    }
+    CK(cudaStreamSynchronize(ctx->st));  // host vectors live on this frame
+    ctx->dirty = true;
+    ctx->may_have_dead = true;
+    *out = m;
+    return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// grid moments for output (meanq_fld_cur, code/output.F90:5222-5482)
+// ---------------------------------------------------------------------------
+extern "C" int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz, float *num,
+                          float *den) {
+    if (!ctx || !num || !den) return TG_ERR_ARG;
+    if (kind < 0 || kind >= TG_MOMENT_KINDS) return fail(ctx, TG_ERR_ARG, "tg_moments: kind %d unknown", kind);
+    if (idx < 0 || idy < 0 || idz < 0) return fail(ctx, TG_ERR_ARG, "tg_moments: negative box half-width");
+    const size_t lot = (size_t)ctx->g.lot;
+    if (!ctx->mom[0]) {
+        int r = dalloc(ctx, &ctx->mom[0], lot);
+        if (!r) r = dalloc(ctx, &ctx->mom[1], lot);
+        if (r) return r;
+        CK(cudaMemsetAsync(ctx->mom[0], 0, lot * 8, ctx->st));
+        CK(cudaMemsetAsync(ctx->mom[1], 0, lot * 8, ctx->st));
+    }
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    float *f3[3] = {ctx->ftmp[0], ctx->ftmp[1], ctx->ftmp[2]};
+    CK(launch_moments(ctx->g, ctx->P, ctx->sp[ctx->par], ctx->d_cnt + 2 * ctx->par, n[0] + n[1], kind, idx, idy,
+                      ctx->g.dims == 3 ? idz : 0, ctx->mom[0], ctx->mom[1], f3, ctx->st));
+    CK(cudaMemcpyAsync(num, f3[0], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(den, f3[1], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     return check_status(ctx);
 }

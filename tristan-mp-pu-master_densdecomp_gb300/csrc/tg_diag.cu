@@ -183,6 +183,118 @@ __global__ void k_diag_finish(double *acc, double *hist, int cap, unsigned long 
     if (threadIdx.x == 0) *counter += 1ull;
 }
 
+// ---------------------------------------------------------------------------
+// grid moments (meanq_fld_cur, code/output.F90:5222-5482): every particle
+// adds its quantity and its weight to the cells of a box around its cell
+// (FP64 atomics, rounded to single once); then the ghost fold, the division
+// by the box size and, for velocity-like moments, by the weight
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void moment_box(const Geom &g, int idx, int idy, int idz, int i, int j, int k, int &lx1,
+                                           int &lx2, int &ly1, int &ly2, int &lz1, int &lz2) {
+    lz1 = max(k - idz, 1);
+    lz2 = min(k + idz, g.mz);
+    if (g.dims == 2) {
+        lz1 = 1;
+        lz2 = 1;
+    }
+    ly1 = max(j - idy, 1);
+    ly2 = min(j + idy, g.my);
+    lx1 = max(i - idx, 1);
+    lx2 = min(i + idx, g.mx);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_moments(Geom g, Species si, Species se, const long long *count, int kind,
+                                                 int idx, int idy, int idz, double *num, double *den) {
+    const long long n0 = count[0], n1 = count[1];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n0 + n1;
+         t += (long long)gridDim.x * blockDim.x) {
+        const bool ion = t < n0;
+        const Species &sp = ion ? si : se;
+        const long long n = ion ? t : t - n0;
+        if (sp.cell[n] < 0) continue;
+        float x, y, z;
+        load_pos<DIM>(g, sp, n, x, y, z);
+        const float u = sp.u[n], v = sp.v[n], w = sp.w[n], ch = sp.ch[n];
+        const float gamprt = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
+        float ax = 0.0f, ay = 0.0f;
+        switch (kind) {
+        case 0: ax = ch; break;
+        case 1: if (ion) ax = ch; break;
+        case 2: ax = u * gamprt * ch; ay = ch; break;
+        case 3: ax = v * gamprt * ch; ay = ch; break;
+        case 4: ax = w * gamprt * ch; ay = ch; break;
+        case 5: if (ion) { ax = u * gamprt * ch; ay = ch; } break;
+        case 6: if (ion) { ax = v * gamprt * ch; ay = ch; } break;
+        case 7: if (ion) { ax = w * gamprt * ch; ay = ch; } break;
+        case 8: ax = u * ch; ay = ch; break;
+        case 9: ax = v * ch; ay = ch; break;
+        case 10: ax = w * ch; ay = ch; break;
+        case 11: if (ion) { ax = u * ch; ay = ch; } break;
+        case 12: if (ion) { ax = v * ch; ay = ch; } break;
+        case 13: if (ion) { ax = w * ch; ay = ch; } break;
+        case 14: if (!ion) { ax = (1.0f / gamprt - 1.0f) * ch; ay = ch; } break;
+        case 15: if (ion) { ax = (1.0f / gamprt - 1.0f) * ch; ay = ch; } break;
+        default: break;
+        }
+        if (ax == 0.0f && ay == 0.0f) continue;
+        int lx1, lx2, ly1, ly2, lz1, lz2;
+        moment_box(g, idx, idy, idz, (int)x, (int)y, DIM == 3 ? (int)z : 1, lx1, lx2, ly1, ly2, lz1, lz2);
+        for (int kk = lz1; kk <= lz2; kk++)
+            for (int jj = ly1; jj <= ly2; jj++)
+                for (int ii = lx1; ii <= lx2; ii++) {
+                    const long long l = lin(g, ii, jj, kk);
+                    if (ax != 0.0f) atomicAdd(num + l, (double)ax);
+                    if (ay != 0.0f) atomicAdd(den + l, (double)ay);
+                }
+    }
+}
+
+__global__ void k_moments_round(long long lot, double *num, double *den, float *fn, float *fd, float *fz) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < lot;
+         t += (long long)gridDim.x * blockDim.x) {
+        fn[t] = __double2float_rn(num[t]);
+        fd[t] = __double2float_rn(den[t]);
+        fz[t] = 0.0f;
+        num[t] = 0.0;
+        den[t] = 0.0;
+    }
+}
+
+__global__ void k_moments_box(Geom g, int kind, int idx, int idy, int idz, float *fn, float *fd) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.lot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.mx) + 1;
+        const long long r = t / g.mx;
+        const int j = (int)(r % g.my) + 1;
+        const int k = (int)(r / g.my) + 1;
+        int lx1, lx2, ly1, ly2, lz1, lz2;
+        moment_box(g, idx, idy, idz, i, j, k, lx1, lx2, ly1, ly2, lz1, lz2);
+        const float box = (float)((lx2 - lx1 + 1) * (ly2 - ly1 + 1) * (lz2 - lz1 + 1));
+        float a = fn[t] / box;
+        const float b = fd[t] / box;
+        if (kind >= 2) a = b != 0.0f ? a / b : 0.0f;
+        fn[t] = a;
+        fd[t] = b;
+    }
+}
+
+static int dgrid(long long n);
+
+cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,
+                           int kind, int idx, int idy, int idz, double *num, double *den, float *const *f3,
+                           cudaStream_t st) {
+    const int grid = dgrid(hint);
+    if (g.dims == 3) k_moments<3><<<grid, 256, 0, st>>>(g, sp[0], sp[1], count, kind, idx, idy, idz, num, den);
+    else k_moments<2><<<grid, 256, 0, st>>>(g, sp[0], sp[1], count, kind, idx, idy, idz, num, den);
+    k_moments_round<<<dgrid(g.lot), 256, 0, st>>>(g.lot, num, den, f3[0], f3[1], f3[2]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if ((e = launch_fold(g, P, f3, st)) != cudaSuccess) return e;
+    k_moments_box<<<dgrid(g.lot), 256, 0, st>>>(g, kind, idx, idy, idz, f3[0], f3[1]);
+    return cudaGetLastError();
+}
+
 static int dgrid(long long n) {
     long long b = (n + 255) / 256;
     if (b < 1) b = 1;

@@ -10,9 +10,9 @@
 // one counting sort over all tiles keeps every box's particles together and
 // grouped by tile. Field kernels run the same per-cell functions as the
 // single-domain kernels over a block table (each CTA takes one chunk of one
-// box); the particle kernel is persistent: one CTA per resident slot pulls
-// tiles from a work queue ordered by expected cost (shape order first) and
-// dispatches on the box's shape order. Per cell and per particle the
+// box); the particle kernels are persistent, one per shape order on
+// concurrent graph branches: one CTA per resident slot pulls tiles from its
+// order's work queue (largest boxes first). Per cell and per particle the
 // arithmetic is that of the single-domain path, so in fixed-point mode every
 // box gives the bits a single-domain run of the same box gives.
 //
@@ -128,9 +128,10 @@ __global__ void __launch_bounds__(256) k_ens_fixed_to_float(const EnsBox *__rest
         fixed_to_float_one(B.fx_inv, fx[0] + o, fx[1] + o, fx[2] + o, f9[6] + o, f9[7] + o, f9[8] + o, t);
 }
 
-// Persistent particle kernel: tiles pulled from the work queue; a CTA keeps
-// the arguments of its current box in shared memory.
-template <bool FIXED>
+// Persistent particle kernel of one shape order: tiles pulled from that
+// order's work queue; a CTA keeps the arguments of its current box in
+// shared memory. The three orders run as concurrent branches of the lap.
+template <int ORDER, bool FIXED>
 __global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
     k_ens_tiles(const TileArgs *__restrict__ boxes, const int2 *__restrict__ work, int nwork, int *queue) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -150,9 +151,7 @@ __global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
             cur = it.x;
         }
         __syncthreads();
-        if (sa.g.order == 1) tile_body<2, 1, FIXED, true, true>(sa, it.y, smem_raw);
-        else if (sa.g.order == 2) tile_body<2, 2, FIXED, true, true>(sa, it.y, smem_raw);
-        else tile_body<2, 3, FIXED, true, true>(sa, it.y, smem_raw);
+        tile_body<2, ORDER, FIXED, true, true>(sa, it.y, smem_raw);
         __syncthreads();  // window and arguments free for the next tile
     }
 }
@@ -227,7 +226,7 @@ struct tg_ens {
     bool fixed = false;
     int sort_every = 1, ntimes = 4;
     size_t smem = 0;
-    int tile_grid = 0;
+    int tile_grid[3] = {0, 0, 0};  // per shape order
     cudaStream_t st = nullptr;
     int device = 0;
     float *f[9] = {};
@@ -248,7 +247,9 @@ struct tg_ens {
     int *d_tofs = nullptr;
     TileArgs *d_targs = nullptr;  // [parity][count tiles][box]
     int2 *d_work = nullptr;
-    int nwork = 0;
+    int wstart[3] = {0, 0, 0}, nwork[3] = {0, 0, 0};  // per shape order: segment of d_work
+    cudaStream_t side[2] = {nullptr, nullptr};       // branches for orders 2 and 1
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
     int2 *d_blk[EK_N] = {};
     int nblk[EK_N] = {};
     // host bindings
@@ -467,7 +468,7 @@ extern "C" int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out) {
         if (!r) r = ealloc(E, &E->cursor[s], (size_t)E->T);
     }
     if (!r) r = ealloc(E, &E->d_status, 1);
-    if (!r) r = ealloc(E, &E->queue, 1);
+    if (!r) r = ealloc(E, &E->queue, 3);
     if (!r) r = ealloc(E, &E->d_box, (size_t)nbox);
     if (!r) r = ealloc(E, &E->d_geom, (size_t)nbox);
     if (!r) r = ealloc(E, &E->d_tofs, (size_t)nbox + 1);
@@ -540,14 +541,30 @@ extern "C" int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out) {
     }
     // persistent grid of the particle kernel: every resident slot
     if (!r) {
-        int nsm = 0, per_sm = 0;
-        auto kern = E->fixed ? k_ens_tiles<true> : k_ens_tiles<false>;
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, E->smem);
+        int nsm = 0, per_sm = 1;
+        void (*kerns[3])(const TileArgs *, const int2 *, int, int *);
+        if (E->fixed) {
+            kerns[0] = k_ens_tiles<1, true>;
+            kerns[1] = k_ens_tiles<2, true>;
+            kerns[2] = k_ens_tiles<3, true>;
+        } else {
+            kerns[0] = k_ens_tiles<1, false>;
+            kerns[1] = k_ens_tiles<2, false>;
+            kerns[2] = k_ens_tiles<3, false>;
+        }
+        e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E->device);
+        for (int o = 0; o < 3 && e == cudaSuccess && per_sm >= 1; o++) {
+            e = cudaFuncSetAttribute(kerns[o], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[o], 256, E->smem);
+            E->tile_grid[o] = nsm * per_sm;
+        }
+        for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+            e = cudaStreamCreateWithFlags(&E->side[b], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->join[b], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->fork, cudaEventDisableTiming);
         if (e != cudaSuccess) r = efail(E, TG_ERR_CUDA, "tg_ens_init: %s", cudaGetErrorString(e));
         else if (per_sm < 1) r = efail(E, TG_ERR_ARG, "tg_ens_init: deposit window of %zu bytes does not fit", E->smem);
-        E->tile_grid = nsm * per_sm;
     }
     if (!r) {
         cudaStream_t st = E->st;
@@ -592,6 +609,11 @@ extern "C" void tg_ens_finalize(tg_ens *E) {
     for (int p = 0; p < 2; p++)
         if (E->cycle[p]) cudaGraphExecDestroy(E->cycle[p]);
     for (void *q : E->allocs) cudaFree(q);
+    for (int b = 0; b < 2; b++) {
+        if (E->side[b]) cudaStreamDestroy(E->side[b]);
+        if (E->join[b]) cudaEventDestroy(E->join[b]);
+    }
+    if (E->fork) cudaEventDestroy(E->fork);
     if (E->st) cudaStreamDestroy(E->st);
     delete E;
 }
@@ -634,9 +656,16 @@ static int build_work(tg_ens *E, const std::vector<long long> &nb) {
     });
     std::vector<int2> work;
     work.reserve(E->T);
-    for (int b : order)
+    for (int o = 0; o < 3; o++) {
+        E->nwork[o] = 0;
+        E->wstart[o] = 0;
+    }
+    for (int b : order) {
+        const int o = E->g[b].order - 1;
+        if (E->nwork[o] == 0) E->wstart[o] = (int)work.size();
         for (int t = 0; t < E->g[b].ntiles; t++) work.push_back(make_int2(b, t));
-    E->nwork = (int)work.size();
+        E->nwork[o] += E->g[b].ntiles;
+    }
     ECK(cudaMemcpyAsync(E->d_work, work.data(), work.size() * sizeof(int2), cudaMemcpyHostToDevice, E->st));
     ECK(cudaStreamSynchronize(E->st));
     return TG_OK;
@@ -817,14 +846,36 @@ static int ens_lap(tg_ens *E, bool sort_now, int *nk) {
     TG_EGHOST(3);
     if (!E->fixed)
         for (int a = 6; a < 9; a++) ECK(cudaMemsetAsync(E->f[a], 0, (size_t)E->ncell * 4, st));
-    ECK(cudaMemsetAsync(E->queue, 0, sizeof(int), st));
+    ECK(cudaMemsetAsync(E->queue, 0, 3 * sizeof(int), st));
     const TileArgs *ta = E->d_targs + (size_t)(E->par * 2 + (sort_now ? 1 : 0)) * E->nbox;
-    if (E->fixed)
-        k_ens_tiles<true><<<E->tile_grid, 256, E->smem, st>>>(ta, E->d_work, E->nwork, E->queue);
-    else
-        k_ens_tiles<false><<<E->tile_grid, 256, E->smem, st>>>(ta, E->d_work, E->nwork, E->queue);
-    ECK(cudaGetLastError());
-    k++;
+    // shape order 3 on the lap's stream, orders 2 and 1 on two branches that
+    // fill the SMs as the order-3 tiles drain
+    ECK(cudaEventRecord(E->fork, st));
+    for (int b = 0; b < 2; b++) ECK(cudaStreamWaitEvent(E->side[b], E->fork, 0));
+    for (int o = 3; o >= 1; o--) {
+        cudaStream_t so = o == 3 ? st : E->side[o == 2 ? 0 : 1];
+        const int2 *w = E->d_work + E->wstart[o - 1];
+        const int nw = E->nwork[o - 1];
+        int *qu = E->queue + (o - 1);
+        const int grid = E->tile_grid[o - 1];
+        if (nw > 0) {
+            if (E->fixed) {
+                if (o == 3) k_ens_tiles<3, true><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+                else if (o == 2) k_ens_tiles<2, true><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+                else k_ens_tiles<1, true><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+            } else {
+                if (o == 3) k_ens_tiles<3, false><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+                else if (o == 2) k_ens_tiles<2, false><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+                else k_ens_tiles<1, false><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
+            }
+            ECK(cudaGetLastError());
+            k++;
+        }
+    }
+    for (int b = 0; b < 2; b++) {
+        ECK(cudaEventRecord(E->join[b], E->side[b]));
+        ECK(cudaStreamWaitEvent(st, E->join[b], 0));
+    }
     TG_EADV(k_ens_advance_b, EK_ADVB);
     TG_EGHOST(3);
     TG_EADV(k_ens_advance_e, EK_ADVE);

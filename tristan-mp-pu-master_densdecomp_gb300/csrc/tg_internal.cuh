@@ -459,6 +459,11 @@ struct DiagLaunch {
     bool particles;  // false: the lap's tile kernel already summed the particles
 };
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
+// grid moments (meanq_fld_cur) into f3[0] (moment) and f3[1] (weight);
+// num / den are zeroed FP64 scratch of g.lot cells, left zeroed
+cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,
+                           int kind, int idx, int idy, int idz, double *num, double *den, float *const *f3,
+                           cudaStream_t st);
 
 // shock hooks (tg_shock.cu)
 cudaError_t launch_field_bc(const Geom &g, const ShockParams &K, float *const *f, cudaStream_t st);

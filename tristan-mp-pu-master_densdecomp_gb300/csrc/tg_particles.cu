@@ -138,42 +138,66 @@ struct AoS {
     int32_t ind, proc, splitlev;
 };
 
+// Records pass through shared memory, so the AoS side moves as contiguous
+// 8-byte words: coalesced in device memory and across NVLink-C2C when the
+// records are host memory read or written in place. Each CTA converts
+// chunks of TG_AOS_CHUNK records (40 B each; a chunk is 1280 words).
+#define TG_AOS_CHUNK 256
 template <int DIM>
-__global__ void k_aos_to_soa(Geom g, const AoS *in, Species sp, long long count, int *status) {
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < count;
-         n += (long long)gridDim.x * blockDim.x) {
-        const AoS p = in[n];
-        int i, j, k;
-        if (pos_cell<DIM>(g, p.x, p.y, p.z, i, j, k)) {
-            store_pos<DIM>(g, sp, n, p.x, p.y, p.z, i, j, k);
-        } else {
-            atomicOr(status, ST_BOUNDS);
-            sp.cell[n] = -1;
+__global__ void __launch_bounds__(TG_AOS_CHUNK)
+    k_aos_to_soa(Geom g, const AoS *in, Species sp, long long count, int *status) {
+    __shared__ unsigned long long buf[TG_AOS_CHUNK * 5];
+    for (long long c0 = blockIdx.x * (long long)TG_AOS_CHUNK; c0 < count;
+         c0 += (long long)gridDim.x * TG_AOS_CHUNK) {
+        const int nrec = (int)min((long long)TG_AOS_CHUNK, count - c0);
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(in + c0);
+        for (int t = threadIdx.x; t < nrec * 5; t += TG_AOS_CHUNK) buf[t] = src[t];
+        __syncthreads();
+        if (threadIdx.x < nrec) {
+            const long long n = c0 + threadIdx.x;
+            const AoS p = *reinterpret_cast<const AoS *>(buf + 5 * threadIdx.x);
+            int i, j, k;
+            if (pos_cell<DIM>(g, p.x, p.y, p.z, i, j, k)) {
+                store_pos<DIM>(g, sp, n, p.x, p.y, p.z, i, j, k);
+            } else {
+                atomicOr(status, ST_BOUNDS);
+                sp.cell[n] = -1;
+            }
+            sp.u[n] = p.u;
+            sp.v[n] = p.v;
+            sp.w[n] = p.w;
+            sp.ch[n] = p.ch;
+            sp.ind[n] = p.ind;
+            sp.proc[n] = p.proc;
+            sp.splitlev[n] = p.splitlev;
         }
-        sp.u[n] = p.u;
-        sp.v[n] = p.v;
-        sp.w[n] = p.w;
-        sp.ch[n] = p.ch;
-        sp.ind[n] = p.ind;
-        sp.proc[n] = p.proc;
-        sp.splitlev[n] = p.splitlev;
+        __syncthreads();
     }
 }
 
 template <int DIM>
-__global__ void k_soa_to_aos(Geom g, Species sp, AoS *out, long long count) {
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < count;
-         n += (long long)gridDim.x * blockDim.x) {
-        AoS p;
-        load_pos<DIM>(g, sp, n, p.x, p.y, p.z);
-        p.u = sp.u[n];
-        p.v = sp.v[n];
-        p.w = sp.w[n];
-        p.ch = sp.ch[n];
-        p.ind = sp.ind[n];
-        p.proc = sp.proc[n];
-        p.splitlev = sp.splitlev[n];
-        out[n] = p;
+__global__ void __launch_bounds__(TG_AOS_CHUNK) k_soa_to_aos(Geom g, Species sp, AoS *out, long long count) {
+    __shared__ unsigned long long buf[TG_AOS_CHUNK * 5];
+    for (long long c0 = blockIdx.x * (long long)TG_AOS_CHUNK; c0 < count;
+         c0 += (long long)gridDim.x * TG_AOS_CHUNK) {
+        const int nrec = (int)min((long long)TG_AOS_CHUNK, count - c0);
+        if (threadIdx.x < nrec) {
+            const long long n = c0 + threadIdx.x;
+            AoS p;
+            load_pos<DIM>(g, sp, n, p.x, p.y, p.z);
+            p.u = sp.u[n];
+            p.v = sp.v[n];
+            p.w = sp.w[n];
+            p.ch = sp.ch[n];
+            p.ind = sp.ind[n];
+            p.proc = sp.proc[n];
+            p.splitlev = sp.splitlev[n];
+            *reinterpret_cast<AoS *>(buf + 5 * threadIdx.x) = p;
+        }
+        __syncthreads();
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(out + c0);
+        for (int t = threadIdx.x; t < nrec * 5; t += TG_AOS_CHUNK) dst[t] = buf[t];
+        __syncthreads();
     }
 }
 
@@ -246,6 +270,7 @@ cudaError_t launch_reorder_keys(const Geom &g, const Species &sp, long long coun
 cudaError_t launch_aos_to_soa(const Geom &g, const void *in, const Species &sp, long long count, int *status,
                               cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
+    if ((uintptr_t)in & 7) return cudaErrorMisalignedAddress;  // records move as 8-byte words
     if (g.dims == 3)
         k_aos_to_soa<3><<<grid_for(count, 256), 256, 0, st>>>(g, (const AoS *)in, sp, count, status);
     else
@@ -255,6 +280,7 @@ cudaError_t launch_aos_to_soa(const Geom &g, const void *in, const Species &sp, 
 
 cudaError_t launch_soa_to_aos(const Geom &g, const Species &sp, void *out, long long count, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
+    if ((uintptr_t)out & 7) return cudaErrorMisalignedAddress;  // records move as 8-byte words
     if (g.dims == 3) k_soa_to_aos<3><<<grid_for(count, 256), 256, 0, st>>>(g, sp, (AoS *)out, count);
     else k_soa_to_aos<2><<<grid_for(count, 256), 256, 0, st>>>(g, sp, (AoS *)out, count);
     return cudaGetLastError();

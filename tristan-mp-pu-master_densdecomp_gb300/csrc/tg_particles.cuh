@@ -155,24 +155,34 @@ struct WindowSink {
     int *status;
     __device__ __forceinline__ void add(int comp, int i, int j, int k, float v) {
         const int a = i - wx0, b = j - wy0, c = k - wz0;
-        if ((unsigned)a < (unsigned)wx && (unsigned)b < (unsigned)wy && (unsigned)c < (unsigned)wz) {
-            const int idx = comp * wcells + a + wx * (b + wy * c);
-            const float x = v * scale;
-            if (fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact split path
-                fx_add_shared(lo, hi, idx, to_fixed32(x));
-                return;
-            }
+        const bool in = (unsigned)a < (unsigned)wx && (unsigned)b < (unsigned)wy && (unsigned)c < (unsigned)wz;
+        add_at(comp, a + wx * (b + wy * c), in, i, j, k, v);
+    }
+    // the box [i0, i0+ni) x [j0, j0+nj) x [k0, k0+nk) lies inside the window
+    __device__ __forceinline__ bool fits(int i0, int j0, int k0, int ni, int nj, int nk) const {
+        return i0 >= wx0 && j0 >= wy0 && k0 >= wz0 && i0 + ni <= wx0 + wx && j0 + nj <= wy0 + wy &&
+               k0 + nk <= wz0 + wz;
+    }
+    // window index of cell (i, j, k), meaningful when it lies in the window
+    __device__ __forceinline__ int index(int i, int j, int k) const {
+        return (i - wx0) + wx * ((j - wy0) + wy * (k - wz0));
+    }
+    // add v at window index widx when in (the cell is in the window),
+    // otherwise at cell (i, j, k) of the global arrays
+    __device__ __forceinline__ void add_at(int comp, int widx, bool in, int i, int j, int k, float v) {
+        const float x = v * scale;
+        if (in && fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact split path
+            fx_add_shared(lo, hi, comp * wcells + widx, to_fixed32(x));
+            return;
         }
-        {
-            // outside the tile window: straight to global memory
-            if (i < 1 || i > g->mx || j < 1 || j > g->my || k < 1 || k > g->mz) {
-                atomicOr(status, ST_BOUNDS);
-                return;
-            }
-            const int l = (i - 1) + (int)g->sy * ((j - 1) + g->my * (k - 1));
-            if (FIXED) atomicAdd(gf[comp] + l, (unsigned long long)to_fixed(v * scale));
-            else atomicAdd(gc[comp] + l, v);
+        // outside the tile window: straight to global memory
+        if (i < 1 || i > g->mx || j < 1 || j > g->my || k < 1 || k > g->mz) {
+            atomicOr(status, ST_BOUNDS);
+            return;
         }
+        const int l = (i - 1) + (int)g->sy * ((j - 1) + g->my * (k - 1));
+        if (FIXED) atomicAdd(gf[comp] + l, (unsigned long long)to_fixed(v * scale));
+        else atomicAdd(gc[comp] + l, v);
     }
 };
 
@@ -289,12 +299,16 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
 
     if (DIM == 2) {
         const float deltaz = z2 - z1;
+        // the whole stencil in the tile window (almost always): cells are
+        // addressed from the row's window index, without per-cell checks
+        const bool in = sink.fits(ibase, jbase, 1, nx, ny, 1);
         // rows rolled (code size), the row's cells unrolled (carries in registers)
 #pragma unroll 1
         for (int ry = 0; ry < ny; ry++) {
             {
                 const float s1y = sel<U>(S1y, ry), dSy = sel<U>(S2y, ry) - s1y;
                 const float wy = s1y + TG_HALF * dSy;
+                const int row = sink.index(ibase, jbase + ry, 1);
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
                     if (rx < nx) {
@@ -304,9 +318,9 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
                         const float cz = -(q * deltaz *
                                            (s1x * s1y + TG_HALF * dSx * s1y + TG_HALF * s1x * dSy +
                                             TG_THIRD * dSx * dSy));
-                        sink.add(0, ibase + rx, jbase + ry, 1, cx);
-                        sink.add(1, ibase + rx, jbase + ry, 1, cy);
-                        sink.add(2, ibase + rx, jbase + ry, 1, cz);
+                        sink.add_at(0, row + rx, in, ibase + rx, jbase + ry, 1, cx);
+                        sink.add_at(1, row + rx, in, ibase + rx, jbase + ry, 1, cy);
+                        sink.add_at(2, row + rx, in, ibase + rx, jbase + ry, 1, cz);
                         cxp = cx;
                         cyp[rx] = cy;
                     }
@@ -323,6 +337,7 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
         const int loz = min(b1z, b2z);
         const int nz = max(b1z, b2z) + NS - loz;
         const int kbase = k1 - 3 + loz;
+        const bool in = sink.fits(ibase, jbase, kbase, nx, ny, nz);
         float S1z[U], S2z[U];
 #pragma unroll
         for (int r = 0; r < U; r++) {
@@ -351,14 +366,15 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
                 const float s1y = sel<U>(S1y, ry);
                 const float dSy = sel<U>(S2y, ry) - s1y;
                 const float wyz = s1y * s1z + TG_HALF * dSy * s1z + TG_HALF * s1y * dSz + TG_THIRD * dSy * dSz;
+                const int row = sink.index(ibase, jbase + ry, kbase + rz);
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
                     if (rx < nx) {
                         const float dSx = S2x[rx] - S1x[rx];
                         const float cx = q * (dSx * wyz) + cxp;
                         const float cy = q * (dSy * wxz[rx]) + cyp[rx];
-                        sink.add(0, ibase + rx, jbase + ry, kbase + rz, cx);
-                        sink.add(1, ibase + rx, jbase + ry, kbase + rz, cy);
+                        sink.add_at(0, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cx);
+                        sink.add_at(1, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cy);
                         cxp = cx;
                         cyp[rx] = cy;
                     }
@@ -381,11 +397,12 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
             for (int rz = 0; rz < nz; rz++) {
                 const float s1z = sel<U>(S1z, rz);
                 const float dSz = sel<U>(S2z, rz) - s1z;
+                const int row = sink.index(ibase, jbase + ry, kbase + rz);
 #pragma unroll
                 for (int rx = 0; rx < U; rx++) {
                     if (rx < nx) {
                         const float cz = q * (dSz * wxy[rx]) + czp[rx];
-                        sink.add(2, ibase + rx, jbase + ry, kbase + rz, cz);
+                        sink.add_at(2, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cz);
                         czp[rx] = cz;
                     }
                 }
@@ -428,21 +445,25 @@ __device__ __forceinline__ void rho_deposit(const Geom &g, float fx_scale, int i
     if (DIM == 3) shape<ORDER>(oz, wz, bz);
     else wz[0] = 1.0f;
     constexpr int NZ = DIM == 3 ? NS : 1;
+    // the whole NS^dims box in the window (almost always): nodes are
+    // addressed from the row's window index without per-node checks
+    const int ra0 = i - 3 + bx - wx0, rb0 = j - 3 + by - wy0, rc0 = (DIM == 3 ? k - 3 + bz : 1) - wz0;
+    const bool in = use_win && ra0 >= 0 && rb0 >= 0 && rc0 >= 0 && ra0 + NS <= g.wx && rb0 + NS <= g.wy &&
+                    rc0 + NZ <= g.wz;
 #pragma unroll 1
     for (int c = 0; c < NZ; c++) {
         const float wzc = sel<NS>(wz, c);
 #pragma unroll
         for (int b = 0; b < NS; b++) {
             const float qyz = q * wy[b] * wzc;
+            const int row = ra0 + g.wx * (rb0 + b + g.wy * (rc0 + c));
 #pragma unroll
             for (int aa = 0; aa < NS; aa++) {
                 const float xs = qyz * wx[aa] * fx_scale;
-                const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
-                const int ra = ii - wx0, rb = jj - wy0, rc = kk - wz0;
-                if (use_win && fabsf(xs) < 1073741824.0f && (unsigned)ra < (unsigned)g.wx &&
-                    (unsigned)rb < (unsigned)g.wy && (unsigned)rc < (unsigned)g.wz) {
-                    fx_add_shared(rlo, rhi, ra + g.wx * (rb + g.wy * rc), to_fixed32(xs));
+                if (in && fabsf(xs) < 1073741824.0f) {
+                    fx_add_shared(rlo, rhi, row + aa, to_fixed32(xs));
                 } else {
+                    const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
                     atomicAdd(rhofx + interior_index<DIM>(g, ii, jj, kk), (unsigned long long)to_fixed(xs));
                 }
             }

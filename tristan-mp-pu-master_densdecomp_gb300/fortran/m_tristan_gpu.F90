@@ -12,10 +12,14 @@
 !
 #ifdef twoD
 module m_tristan_gpu
+  use m_system
+  use m_aux
   use m_fields
   use m_particles
 #else
 module m_tristan_gpu_3d
+  use m_system_3d
+  use m_aux_3d
   use m_fields_3d
   use m_particles_3d
 #endif
@@ -35,6 +39,22 @@ module m_tristan_gpu_3d
      integer(c_int64_t) :: maxhlf
      integer(c_int32_t) :: sort_every, tile(3), device, diag_every
   end type tg_config
+
+  type, bind(C) :: tg_shock
+     integer(c_int32_t) :: wall
+     real(c_double) :: walloc
+     real(c_float) :: gammawall, betawall
+     integer(c_int32_t) :: cond_i1, cond_i2, edge_i1, edge_i2
+     real(c_float) :: edge(6)
+     integer(c_int32_t) :: inject
+     real(c_double) :: xinject2
+     real(c_float) :: betainj
+     real(c_double) :: xinj_max
+     real(c_float) :: ppc0, gamma_drift, weight, y1, y2, delgam_i, delgam_e, pcosthmult
+     integer(c_int32_t) :: sigma_nonzero
+     real(c_double) :: dseed
+     integer(c_int32_t) :: totalpartnum
+  end type tg_shock
 
   interface
      integer(c_int) function tg_init(cfg, ctx) bind(C, name="tg_init")
@@ -118,7 +138,64 @@ module m_tristan_gpu_3d
        type(c_ptr), value :: ctx
        integer(c_int32_t), value :: nsteps
      end function
+     ! collisionless-shock hooks (user_pu/user_shock_pu.F90)
+     integer(c_int) function tg_shock_init(ctx, k) bind(C, name="tg_shock_init")
+       import :: c_int, c_ptr, tg_shock
+       type(c_ptr), value :: ctx
+       type(tg_shock), intent(in) :: k
+     end function
+     integer(c_int) function tg_shock_get(ctx, k) bind(C, name="tg_shock_get")
+       import :: c_int, c_ptr, tg_shock
+       type(c_ptr), value :: ctx
+       type(tg_shock), intent(out) :: k
+     end function
+     integer(c_int) function tg_inject_region(ctx, x1, x2, y1, y2, ppc, weight) bind(C, name="tg_inject_region")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: ctx
+       real(c_float), value :: x1, x2, y1, y2, ppc, weight
+     end function
+     integer(c_int) function tg_particle_bc(ctx) bind(C, name="tg_particle_bc")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_field_bc(ctx) bind(C, name="tg_field_bc")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     integer(c_int) function tg_inject(ctx) bind(C, name="tg_inject")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
+     ! restart files and output moments
+     integer(c_int) function tg_write_restart(ctx, ffld, fprt, meta) bind(C, name="tg_write_restart")
+       import :: c_int, c_ptr, c_char, tg_restart_meta
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: ffld(*), fprt(*)
+       type(tg_restart_meta), intent(in) :: meta
+     end function
+     integer(c_int) function tg_read_restart(ctx, ffld, fprt, meta) bind(C, name="tg_read_restart")
+       import :: c_int, c_ptr, c_char, tg_restart_meta
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: ffld(*), fprt(*)
+       type(tg_restart_meta), intent(out) :: meta
+     end function
+     integer(c_int) function tg_moments(ctx, kind, idx, idy, idz, num, den) bind(C, name="tg_moments")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: kind, idx, idy, idz
+       type(c_ptr), value :: num, den
+     end function
   end interface
+
+  type, bind(C) :: tg_restart_meta
+     real(c_double) :: dseed
+     integer(c_int32_t) :: lap
+     real(c_double) :: xinject, xinject2, xinject3
+     real(c_float) :: leftwall
+     real(c_double) :: walloc
+     integer(c_int32_t) :: totalpartnum, maxptl
+     integer(c_int64_t) :: max_subrecord
+  end type tg_restart_meta
 
   type(c_ptr), save :: ctx = c_null_ptr
   integer(c_int), parameter :: SYNC_E = 1, SYNC_B = 2, SYNC_CUR = 4, SYNC_PARTICLES = 8, SYNC_ALL = 15
@@ -126,7 +203,9 @@ module m_tristan_gpu_3d
   public :: tg_start, tg_stop, tg_download, tg_upload, &
             gpu_bc_b1, gpu_bc_e1, gpu_advance_Bhalfstep, gpu_advance_Efield, gpu_move_particles, &
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
-            gpu_add_current, gpu_reorder_particles, gpu_step
+            gpu_add_current, gpu_reorder_particles, gpu_step, &
+            gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
+            gpu_write_restart, gpu_read_restart, gpu_meanq
 
 contains
 
@@ -229,6 +308,42 @@ contains
   end subroutine
   subroutine gpu_reorder_particles()
     call check(tg_reorder(ctx, int(lap, c_int32_t), 0_c_int32_t), "reorder_particles")
+  end subroutine
+
+  ! the shock's user hooks on the device (after tg_shock_init)
+  subroutine gpu_particle_bc_user()
+    call check(tg_particle_bc(ctx), "particle_bc_user")
+  end subroutine
+  subroutine gpu_field_bc_user()
+    call check(tg_field_bc(ctx), "field_bc_user")
+  end subroutine
+  subroutine gpu_inject_particles_user()
+    call check(tg_inject(ctx), "inject_particles_user")
+  end subroutine
+
+  ! write_restart / restart with the device state (frestartfld, frestartprt)
+  subroutine gpu_write_restart(ffld, fprt)
+    character(len=*), intent(in) :: ffld, fprt
+    type(tg_restart_meta) :: m
+    m%dseed = dseed; m%lap = lap; m%xinject = xinject; m%xinject2 = xinject2; m%xinject3 = xinject3
+    m%leftwall = leftwall; m%walloc = walloc; m%totalpartnum = totalpartnum; m%maxptl = maxptl
+    m%max_subrecord = 0
+    call check(tg_write_restart(ctx, trim(ffld)//c_null_char, trim(fprt)//c_null_char, m), "write_restart")
+  end subroutine
+  subroutine gpu_read_restart(ffld, fprt)
+    character(len=*), intent(in) :: ffld, fprt
+    type(tg_restart_meta) :: m
+    call check(tg_read_restart(ctx, trim(ffld)//c_null_char, trim(fprt)//c_null_char, m), "restart")
+    dseed = m%dseed; lapst = m%lap + 1; xinject = m%xinject; xinject2 = m%xinject2; xinject3 = m%xinject3
+    leftwall = m%leftwall; walloc = m%walloc; totalpartnum = m%totalpartnum
+  end subroutine
+
+  ! meanq_fld_cur on the device: kind 0..15 in the order of tg_moments
+  subroutine gpu_meanq(kind, num, den)
+    integer, intent(in) :: kind
+    real, target, intent(out) :: num(:,:,:), den(:,:,:)
+    call check(tg_moments(ctx, int(kind, c_int32_t), 2_c_int32_t, 2_c_int32_t, merge(0_c_int32_t, 2_c_int32_t, mz == 1), &
+               c_loc(num), c_loc(den)), "meanq_fld_cur")
   end subroutine
 
   ! the whole periodic lap fused on the device (replaces lines 115-303)

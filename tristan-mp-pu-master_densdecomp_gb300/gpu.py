@@ -89,6 +89,15 @@ def make_tg_shock(sh: dict) -> tg_shock:
     return k
 
 
+class tg_restart_meta(ctypes.Structure):
+    _fields_ = [
+        ("dseed", ctypes.c_double), ("lap", ctypes.c_int32),
+        ("xinject", ctypes.c_double), ("xinject2", ctypes.c_double), ("xinject3", ctypes.c_double),
+        ("leftwall", ctypes.c_float), ("walloc", ctypes.c_double),
+        ("totalpartnum", ctypes.c_int32), ("maxptl", ctypes.c_int32), ("max_subrecord", ctypes.c_int64),
+    ]
+
+
 class tg_diag(ctypes.Structure):
     _fields_ = [
         ("gauss_residual", ctypes.c_double), ("gauss_abs", ctypes.c_double),
@@ -112,7 +121,11 @@ ENTRY_POINTS = (
     "tg_ens_sync_from_host", "tg_ens_sync_to_host", "tg_ens_step", "tg_ens_step_timed", "tg_ens_diag_fp64",
     "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
     "tg_shock_init", "tg_shock_get", "tg_inject_region", "tg_particle_bc", "tg_field_bc", "tg_inject",
+    "tg_write_restart", "tg_read_restart", "tg_moments",
 )
+# grid moments of meanq_fld_cur (code/output.F90:5222-5482), by the reference's names
+MOMENTS = ("tdens", "idens", "tbetx", "tbety", "tbetz", "ibetx", "ibety", "ibetz", "tmomx", "tmomy", "tmomz",
+           "imomx", "imomy", "imomz", "eener", "iener")
 PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
 
 
@@ -177,6 +190,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     for n in ("tg_particle_bc", "tg_field_bc", "tg_inject"):
         getattr(lib, n).argtypes = [P]
         getattr(lib, n).restype = ctypes.c_int
+    lib.tg_moments.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, P, P]
+    lib.tg_moments.restype = ctypes.c_int
+    lib.tg_write_restart.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(tg_restart_meta)]
+    lib.tg_write_restart.restype = ctypes.c_int
+    lib.tg_read_restart.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(tg_restart_meta)]
+    lib.tg_read_restart.restype = ctypes.c_int
     # batched ensemble
     lib.tg_ens_init.argtypes = [ctypes.POINTER(tg_config), ctypes.c_int32, ctypes.POINTER(P)]
     lib.tg_ens_init.restype = ctypes.c_int
@@ -482,6 +501,29 @@ class GpuSim:
 
     def inject_particles_user(self):
         self._check(self.lib.tg_inject(self.h))
+
+    # -- output moments (meanq_fld_cur) ----------------------------------------
+    def meanq(self, name: str, idx: int = 2, idy: int = 2, idz: int = 2):
+        """(moment, box-averaged weight), each mx*my*mz floats"""
+        num = np.zeros(self.lot, np.float32)
+        den = np.zeros(self.lot, np.float32)
+        self._check(self.lib.tg_moments(self.h, MOMENTS.index(name), idx, idy, idz, num.ctypes.data,
+                                        den.ctypes.data))
+        return num, den
+
+    # -- restart files (write_restart / restart) -------------------------------
+    def write_restart(self, fields_path: str, particles_path: str, **meta) -> None:
+        m = tg_restart_meta()
+        for k, v in meta.items():
+            setattr(m, k, v)
+        self._check(self.lib.tg_write_restart(self.h, fields_path.encode(), particles_path.encode(),
+                                              ctypes.byref(m)))
+
+    def read_restart(self, fields_path: str, particles_path: str) -> dict:
+        m = tg_restart_meta()
+        self._check(self.lib.tg_read_restart(self.h, fields_path.encode(), particles_path.encode(),
+                                             ctypes.byref(m)))
+        return {k: getattr(m, k) for k, _ in tg_restart_meta._fields_}
 
 
 def _diag_dict(d: tg_diag) -> dict:
