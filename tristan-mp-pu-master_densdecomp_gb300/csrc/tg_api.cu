@@ -38,6 +38,8 @@ struct tg_ctx {
     long long hcount[2] = {0, 0};
     int *tstart[2] = {}, *hist[2] = {}, *cursor[2] = {};
     int *d_status = nullptr;
+    int *d_dead = nullptr;  // a particle was dropped on purpose since the last sort
+    bool fault_seen = false;  // a reported device fault may have dropped particles
     bool dirty = true;      // particles not grouped by tile
     bool may_have_dead = false;  // entries marked discarded since the last sort
     // host bindings
@@ -112,6 +114,7 @@ static int check_status(tg_ctx *ctx) {
     CK(cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if (st == 0) return TG_OK;
+    ctx->fault_seen = true;
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->st));
     if (st & ST_NAN) return fail(ctx, TG_ERR_NAN, "non-finite particle coordinate (device status %d)", st);
     if (st & ST_OVERFLOW) return fail(ctx, TG_ERR_OVERFLOW, "particle capacity exceeded (device status %d)", st);
@@ -278,6 +281,7 @@ extern "C" int tg_init(const tg_config *cfg, tg_ctx **out) {
         if (!r) r = dalloc(ctx, &ctx->cursor[s], (size_t)g.ntiles);
     }
     if (!r) r = dalloc(ctx, &ctx->d_status, 1);
+    if (!r) r = dalloc(ctx, &ctx->d_dead, 1);
     {
         const size_t nint = (size_t)(g.mx - g.ng) * (g.my - g.ng) * (g.dims == 3 ? g.mz - g.ngz : 1);
         if (!r) r = dalloc(ctx, &ctx->rhofx, nint);
@@ -310,6 +314,7 @@ extern "C" int tg_init(const tg_config *cfg, tg_ctx **out) {
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_cnt, 0, 4 * sizeof(long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_status, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_dead, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         fail(nullptr, TG_ERR_CUDA, "tg_init: %s", cudaGetErrorString(e));
@@ -382,6 +387,8 @@ static int sort_all(tg_ctx *ctx, bool counted) {
     int r;
     if ((r = sort_species(ctx, 0, counted))) return r;
     if ((r = sort_species(ctx, 1, counted))) return r;
+    CK(cudaMemsetAsync(ctx->d_dead, 0, sizeof(int), ctx->st));
+    ctx->fault_seen = false;
     ctx->par ^= 1;
     ctx->dirty = false;
     ctx->may_have_dead = false;
@@ -412,6 +419,7 @@ static TileArgs tile_args(tg_ctx *ctx, bool count_tiles) {
         a.fix[cc] = ctx->fix[cc];
     }
     a.status = ctx->d_status;
+    a.dead = ctx->d_dead;
     if (ctx->shock_on) {
         a.shock = ctx->d_shock;
         a.wall = ctx->K.wall;
@@ -442,21 +450,17 @@ extern "C" int tg_bind_particles(tg_ctx *ctx, void *p, int32_t *ions, int32_t *l
 
 static const size_t AOS = 40;
 
-// A device-usable view of a host array: the device pointer of page-locked
-// (registered) memory, or the pointer itself when the device reads pageable
-// host memory coherently (NVLink-C2C systems); NULL otherwise (staged
-// copies are used then).
+// A device-usable view of a page-locked (registered or pinned) host array:
+// its device pointer, so the conversion kernels read and write the records
+// in place at the link's bandwidth; NULL for pageable memory (staged copies
+// are used then: a kernel walking pageable memory through the host page
+// tables is far slower than a staged copy).
 static void *host_view(tg_ctx *ctx, void *h) {
+    (void)ctx;
     if ((uintptr_t)h & 7) return nullptr;  // the conversion kernels move 8-byte words
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, h) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
         return at.devicePointer;
-    (void)cudaGetLastError();
-    int pageable = 0;
-    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device) ==
-            cudaSuccess &&
-        pageable)
-        return h;
     (void)cudaGetLastError();
     return nullptr;
 }
@@ -507,8 +511,18 @@ extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
 // order of a buffer without discarded entries is left as it is)
 static int exact_counts(tg_ctx *ctx, long long n[2]) {
     if (ctx->may_have_dead) {
-        int r = sort_all(ctx, false);
-        if (r) return r;
+        // dropped entries exist only after a deliberate drop or a reported
+        // fault; otherwise the buffer is already compact
+        int flags[2] = {1, 1};
+        CK(cudaMemcpyAsync(&flags[0], ctx->d_dead, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(&flags[1], ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        if (flags[0] != 0 || flags[1] != 0 || ctx->fault_seen) {
+            int r = sort_all(ctx, false);
+            if (r) return r;
+        } else {
+            ctx->may_have_dead = false;
+        }
     }
     CK(cudaMemcpyAsync(n, ctx->d_cnt + 2 * ctx->par, 2 * sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -937,7 +951,8 @@ extern "C" int tg_particle_bc(tg_ctx *ctx) {
     if (!ctx->shock_on) return fail(ctx, TG_ERR_STATE, "tg_particle_bc: hooks not set (tg_shock_init)");
     float *cur3[3] = {ctx->f[6], ctx->f[7], ctx->f[8]};
     CK(launch_particle_bc(ctx->g, ctx->P, ctx->K, ctx->d_shock, cur_species(ctx), ctx->d_cnt + 2 * ctx->par,
-                          count_hint(ctx, 0) + count_hint(ctx, 1), cur3, ctx->fix, ctx->d_status, ctx->st));
+                          count_hint(ctx, 0) + count_hint(ctx, 1), cur3, ctx->fix, ctx->d_status, ctx->d_dead,
+                          ctx->st));
     ctx->may_have_dead = true;
     return TG_OK;
 }

@@ -58,27 +58,40 @@ __global__ void __launch_bounds__(256, 4) k_diag_particles(DiagArgs a) {
         // per-thread compensated FP32 sums, one FP64 add per thread and species
         // (GB300 issues FP64 at a small fraction of the FP32 rate)
         float ks[4] = {0, 0, 0, 0}, kc[4] = {0, 0, 0, 0};
-        for (int n = beg + threadIdx.x; n < end; n += blockDim.x) {
-            const int cell = sp.cell[n];
-            if (cell < 0) continue;
+        // the next particle's record is loaded before this one is deposited,
+        // so its memory latency overlaps the deposit
+        int n = beg + threadIdx.x;
+        int cell = n < end ? sp.cell[n] : -1;
+        float ox = 0.f, oy = 0.f, oz = 0.f, ch = 0.f, u = 0.f, v = 0.f, w = 0.f;
+        if (n < end) {
+            ox = sp.ox[n]; oy = sp.oy[n]; oz = DIM == 3 ? sp.oz[n] : 0.0f;
+            ch = sp.ch[n]; u = sp.u[n]; v = sp.v[n]; w = sp.w[n];
+        }
+        while (n < end) {
+            const int ccell = cell;
+            const float cox = ox, coy = oy, coz = oz, cch = ch, cu = u, cv = v, cw = w;
+            n += blockDim.x;
+            if (n < end) {
+                cell = sp.cell[n];
+                ox = sp.ox[n]; oy = sp.oy[n]; oz = DIM == 3 ? sp.oz[n] : 0.0f;
+                ch = sp.ch[n]; u = sp.u[n]; v = sp.v[n]; w = sp.w[n];
+            }
+            if (ccell < 0) continue;
             int i, j, k;
-            cell_ijk(g, cell, i, j, k);
-            const float ox = sp.ox[n], oy = sp.oy[n];
-            const float oz = DIM == 3 ? sp.oz[n] : 0.0f;
-            const float q = sp.ch[n] * qs;
-            rho_deposit<DIM, ORDER>(g, a.P.fx_scale, i, j, k, ox, oy, oz, q, winlo, winhi, wx0, wy0, wz0, use_win,
-                                    a.rhofx);
-            const float u = sp.u[n], v = sp.v[n], w = sp.w[n];
-            const float u2 = u * u + v * v + w * w;
+            cell_ijk(g, ccell, i, j, k);
+            const float q = cch * qs;
+            rho_deposit<DIM, ORDER>(g, a.P.fx_scale, i, j, k, cox, coy, coz, q, winlo, winhi, wx0, wy0, wz0,
+                                    use_win, a.rhofx);
+            const float u2 = cu * cu + cv * cv + cw * cw;
             const float gm1 = u2 / (sqrtf(1.0f + u2) + 1.0f);
-            const float mc = m * sp.ch[n];
-            const float terms[4] = {gm1 * mc, mc * u, mc * v, mc * w};
+            const float mc = m * cch;
+            const float terms[4] = {gm1 * mc, mc * cu, mc * cv, mc * cw};
 #pragma unroll
-            for (int q = 0; q < 4; q++) {  // Kahan summation
-                const float y = terms[q] - kc[q];
-                const float t = ks[q] + y;
-                kc[q] = (t - ks[q]) - y;
-                ks[q] = t;
+            for (int t4 = 0; t4 < 4; t4++) {  // Kahan summation
+                const float y = terms[t4] - kc[t4];
+                const float t = ks[t4] + y;
+                kc[t4] = (t - ks[t4]) - y;
+                ks[t4] = t;
             }
         }
         part[s] += (double)ks[0] - (double)kc[0];

@@ -409,6 +409,9 @@ struct TileArgs {
     const ShockState *shock;
     int wall;
     float gammawall, betawall;
+    // set to 1 when a particle is dropped on purpose (open boundary, wall),
+    // so the host knows the next download must compact (null: not tracked)
+    int *dead;
 };
 
 // ---------------------------------------------------------------------------
@@ -472,7 +475,7 @@ cudaError_t launch_wall_step(const Params &P, const ShockParams &K, ShockState *
 // wall advance and the wall over all particles (particle_bc_user alone)
 cudaError_t launch_particle_bc(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
                                const Species *sp, const long long *count, long long hint, float *const *cur,
-                               unsigned long long *const *fix, int *status, cudaStream_t st);
+                               unsigned long long *const *fix, int *status, int *dead, cudaStream_t st);
 // plan one injection: mode 0 = the moving injector's slab, 1 = the region
 // (x1, x2, y1, y2) with ppc and weight
 cudaError_t launch_inject_plan(const Geom &g, const Params &P, const ShockParams &K, ShockState *S, int mode,

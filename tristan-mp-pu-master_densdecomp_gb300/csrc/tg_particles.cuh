@@ -587,6 +587,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                         !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
                                       y, z, u, v, w)) {
                         sp.cell[n] = -1;  // removed by the wall (dropped by the next sort)
+                        if (a.dead) *a.dead = 1;
                         continue;
                     }
                 }
@@ -611,6 +612,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                     if (a.newcount[s]) agg_inc(a.newcount[s], tile_of(g, i, j, k));
                 } else {
                     if (keep) atomicOr(a.status, ST_BOUNDS);
+                    else if (a.dead) *a.dead = 1;
                     sp.cell[n] = -1;  // discarded: dropped by the next sort
                 }
                 if (PUSH) {

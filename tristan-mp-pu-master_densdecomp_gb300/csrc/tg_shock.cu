@@ -355,7 +355,8 @@ __global__ void k_wall_step(float c, float betawall, ShockState *S) {
 __global__ void __launch_bounds__(256) k_particle_bc(Geom g, Params P, ShockParams K, const ShockState *S,
                                                      Species si, Species se, const long long *count,
                                                      float *c0, float *c1, float *c2, unsigned long long *f0,
-                                                     unsigned long long *f1, unsigned long long *f2, int *status) {
+                                                     unsigned long long *f1, unsigned long long *f2, int *status,
+                                                     int *dead) {
     WindowSink<true> sfx;
     WindowSink<false> s32;
     sfx.lo = s32.lo = nullptr;
@@ -399,6 +400,7 @@ __global__ void __launch_bounds__(256) k_particle_bc(Geom g, Params P, ShockPara
             sp.u[n] = u;
         } else {
             sp.cell[n] = -1;  // removed (dropped by the next sort)
+            *dead = 1;
         }
     }
 }
@@ -453,11 +455,11 @@ cudaError_t launch_field_bc(const Geom &g, const ShockParams &K, float *const *f
 
 cudaError_t launch_particle_bc(const Geom &g, const Params &P, const ShockParams &K, ShockState *S,
                                const Species *sp, const long long *count, long long hint, float *const *cur,
-                               unsigned long long *const *fix, int *status, cudaStream_t st) {
+                               unsigned long long *const *fix, int *status, int *dead, cudaStream_t st) {
     if (!K.wall) return cudaSuccess;
     k_wall_step<<<1, 32, 0, st>>>(P.c, K.betawall, S);
     k_particle_bc<<<grid_for(hint), 256, 0, st>>>(g, P, K, S, sp[0], sp[1], count, cur[0], cur[1], cur[2],
-                                                 fix[0], fix[1], fix[2], status);
+                                                 fix[0], fix[1], fix[2], status, dead);
     return cudaGetLastError();
 }
 
