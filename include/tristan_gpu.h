@@ -331,6 +331,21 @@ int tg_read_restart(tg_ctx *ctx, const char *fields_path, const char *particles_
 #define TG_MOMENT_KINDS 16
 int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz, float *num, float *den);
 
+/* Energy spectra in the local flow frame for the spectrum output
+   (save_spectrum_2d, code/output.F90:794-1249): slices of 30 cells over
+   x in [mx0/2 - 1200, mx0/2 + 400] and the interior in y; the gamma range
+   over every particle; per species the slice-mean velocity, each
+   particle's gamma in that frame, and gambins logarithmic bins of
+   gamma - 1 counting the weights ch. tg_spectrum_dims gives nxbins and
+   nybins; spec_* hold nxbins*nybins*gambins floats (x fastest), xgamma
+   gambins, xslice nxbins, yslice nybins, gamma_range (may be NULL) the
+   [gammin, gammax] used. log10 is evaluated in double and rounded once;
+   slice means are FP64 sums rounded to single (the reference sums in
+   single, particle by particle). Synchronises. */
+int tg_spectrum_dims(tg_ctx *ctx, int32_t gambins, int32_t *nxbins, int32_t *nybins);
+int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *xgamma, float *xslice,
+                float *yslice, float *gamma_range);
+
 /* ---------------------------------------------------------------------
    Batched ensemble: many independent periodic 2D boxes of uneven size
    (seed or parameter ensembles) stepped together, one launch per phase for

@@ -151,6 +151,14 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_meanq.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p]
             lib.to_meanq.restype = None
+            lib.to_log10f.argtypes = [ctypes.c_float]
+            lib.to_log10f.restype = ctypes.c_float
+            lib.to_spectrum_dims.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_int)]
+            lib.to_spectrum_dims.restype = ctypes.c_int
+            lib.to_spectrum_2d.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5 + \
+                [ctypes.POINTER(ctypes.c_float)] * 2
+            lib.to_spectrum_2d.restype = None
             K = ctypes.POINTER(to_shock)
             lib.to_random.argtypes = [ctypes.POINTER(ctypes.c_double)]
             lib.to_random.restype = ctypes.c_float
@@ -297,6 +305,19 @@ class OracleSim:
         self.lib.to_meanq(self.ptr, kind, idx, idy, idz if self.cfg.dims == 3 else 0, num.ctypes.data,
                           den.ctypes.data)
         return num, den
+
+    def spectrum(self, gambins: int = 200) -> dict:
+        nx, ny = ctypes.c_int(), ctypes.c_int()
+        self.lib.to_spectrum_dims(self.ptr, gambins, ctypes.byref(nx), ctypes.byref(ny))
+        si = np.zeros((gambins, ny.value, nx.value), np.float32)
+        se = np.zeros_like(si)
+        xg = np.zeros(gambins, np.float32)
+        xs = np.zeros(nx.value, np.float32)
+        ys = np.zeros(ny.value, np.float32)
+        gmin, gmax = ctypes.c_float(), ctypes.c_float()
+        self.lib.to_spectrum_2d(self.ptr, gambins, si.ctypes.data, se.ctypes.data, xg.ctypes.data, xs.ctypes.data,
+                                ys.ctypes.data, ctypes.byref(gmin), ctypes.byref(gmax))
+        return dict(ions=si, lecs=se, xgamma=xg, xslice=xs, yslice=ys, gammin=gmin.value, gammax=gmax.value)
 
     def charge_density(self) -> np.ndarray:
         rho = np.zeros(self.lot, np.float64)

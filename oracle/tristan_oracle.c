@@ -1586,3 +1586,123 @@ void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, floa
     memcpy(cz, keep + 2 * lot, sizeof(float) * lot);
     free(keep);
 }
+
+/* ------------------------------------------------------------------------
+ * Energy spectra in the flow frame per x-y slice (save_spectrum_2d,
+ * code/output.F90:794-1249): gamma range over all particles, slice means
+ * of the velocity, Lorentz transformation of each particle into its
+ * slice's mean frame, histogram of log10(gamma' - 1) in gambins bins.
+ * log10 of a single is evaluated in double (atanh series after splitting
+ * off the binary exponent) and rounded once.
+ * --------------------------------------------------------------------- */
+float to_log10f(float x)
+{
+    if (!(x > 0.0f)) return x == 0.0f ? -INFINITY : NAN;
+    if (isinf(x)) return x;
+    int e;
+    double m = frexp((double)x, &e); /* x = m 2^e, m in [0.5, 1) */
+    if (m < 0.70710678118654752) {
+        m = m * 2.0;
+        e = e - 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0), s2 = s * s;
+    double t = 1.0 / 23.0;
+    for (int k = 21; k >= 1; k -= 2) t = 1.0 / k + s2 * t;
+    const double ln = 2.0 * s * t + (double)e * 0.69314718055994530942;
+    return (float)(ln / 2.30258509299404568402);
+}
+
+int to_spectrum_dims(const to_state *s, int gambins, int *nx, int *ny)
+{
+    const int ng = s->nghost;
+    const int mxmin = (int)((float)(s->mx - ng) * 0.5f) - 1200 + (ng / 2 + 1);
+    const int mxmax = (int)((float)(s->mx - ng) * 0.5f) + 400 + (ng / 2 + 1);
+    const int mymin = ng / 2 + 1, mymax = s->my - ng / 2;
+    *nx = (mxmax - mxmin) / 30 > 1 ? (mxmax - mxmin) / 30 : 1;
+    *ny = (mymax - mymin) / 30 > 1 ? (mymax - mymin) / 30 : 1;
+    return gambins;
+}
+
+/* spec_i / spec_e: nxbins*nybins*gambins (x fastest); xgamma: gambins;
+   xslice / yslice: nxbins / nybins; returns gammin and gammax */
+void to_spectrum_2d(const to_state *s, int gambins, float *spec_i, float *spec_e, float *xgamma, float *xslice,
+                    float *yslice, float *gmin_out, float *gmax_out)
+{
+    const int ng = s->nghost;
+    const int mxmin = (int)((float)(s->mx - ng) * 0.5f) - 1200 + (ng / 2 + 1);
+    const int mxmax = (int)((float)(s->mx - ng) * 0.5f) + 400 + (ng / 2 + 1);
+    const int mymin = ng / 2 + 1, mymax = s->my - ng / 2;
+    int nxb, nyb;
+    to_spectrum_dims(s, gambins, &nxb, &nyb);
+    const float dxslice = 1.0f * (float)(mxmax - mxmin) / (float)nxb;
+    const float dyslice = 1.0f * (float)(mymax - mymin) / (float)nyb;
+    for (int i = 1; i <= nxb; i++) xslice[i - 1] = dxslice * (float)(i - 1) + 0.5f * dxslice + (float)mxmin;
+    for (int i = 1; i <= nyb; i++) yslice[i - 1] = dyslice * (float)(i - 1) + 0.5f * dyslice + (float)mymin;
+    float gammin = 1.0f, gammax = 1.0f;
+    for (int sp = 0; sp < 2; sp++) {
+        const int64_t base = sp == 0 ? 0 : s->maxhlf, cnt = sp == 0 ? s->ions : s->lecs;
+        for (int64_t n = 0; n < cnt; n++) {
+            const to_particle *p = &s->p[base + n];
+            const float gam = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+            if (gam > gammax) gammax = gam;
+            if (gam < gammin) gammin = gam;
+        }
+    }
+    gammin = fmaxf(gammin, 1.0f + 1e-6f);
+    const float dgam = (to_log10f(gammax - 1.0f) - to_log10f(gammin - 1.0f)) / (float)gambins;
+    for (int i = 1; i <= gambins; i++)
+        xgamma[i - 1] = powf(10.0f, (float)(i - 1) * dgam + to_log10f(gammin - 1.0f));
+    const int64_t nsl = (int64_t)nxb * nyb;
+    float *um = calloc((size_t)nsl * 4, sizeof(float));
+    float *vm = um + nsl, *wm = vm + nsl, *nd = wm + nsl;
+    for (int sp = 0; sp < 2; sp++) {
+        float *spec = sp == 0 ? spec_i : spec_e;
+        memset(spec, 0, sizeof(float) * (size_t)nsl * gambins);
+        memset(um, 0, sizeof(float) * (size_t)nsl * 4);
+        const int64_t base = sp == 0 ? 0 : s->maxhlf, cnt = sp == 0 ? s->ions : s->lecs;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int64_t n = 0; n < cnt; n++) {
+                const to_particle *p = &s->p[base + n];
+                if (p->ind <= 0) continue;
+                const float fxb = (p->x + (float)s->mxcum - (float)mxmin) / dxslice + 1.0f;
+                const float fyb = (p->y + (float)s->mycum - (float)mymin) / dyslice + 1.0f;
+                if (!(fxb >= 1.0f && fyb >= 1.0f)) continue;
+                const int xbin = (int)fxb, ybin = (int)fyb;
+                if (xbin > nxb || ybin > nyb) continue;
+                const int64_t sl = (xbin - 1) + (int64_t)nxb * (ybin - 1);
+                const float gam = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+                if (pass == 0) {
+                    nd[sl] = nd[sl] + p->ch;
+                    um[sl] = um[sl] + (p->u / gam) * p->ch;
+                    vm[sl] = vm[sl] + (p->v / gam) * p->ch;
+                    wm[sl] = wm[sl] + (p->w / gam) * p->ch;
+                    continue;
+                }
+                const float vx = um[sl], vy = vm[sl], vz = wm[sl];
+                const float vr = sqrtf(vx * vx + vy * vy + vz * vz);
+                const float gvr = 1.0f / sqrtf(1.0f - vr * vr);
+                const float vr2 = vr * vr;
+                const float uprime = -vx * gvr * gam + (1.0f + (gvr - 1.0f) * (vx * vx) / vr2) * p->u +
+                                     (gvr - 1.0f) * vx * vy / vr2 * p->v + (gvr - 1.0f) * vx * vz / vr2 * p->w;
+                const float vprime = -vy * gvr * gam + (gvr - 1.0f) * vx * vy / vr2 * p->u +
+                                     (1.0f + (gvr - 1.0f) * (vy * vy) / vr2) * p->v + (gvr - 1.0f) * vy * vz / vr2 * p->w;
+                const float wprime = -vz * gvr * gam + (gvr - 1.0f) * vx * vz / vr2 * p->u +
+                                     (gvr - 1.0f) * vy * vz / vr2 * p->v + (1.0f + (gvr - 1.0f) * (vz * vz) / vr2) * p->w;
+                const float gp = sqrtf(1.0f + (uprime * uprime + vprime * vprime + wprime * wprime));
+                const float fg = (to_log10f(gp - 1.0f) - to_log10f(gammin - 1.0f)) / dgam + 1.0f;
+                if (!(fg >= 1.0f && fg < (float)gambins + 1.0f)) continue;
+                const int gbin = (int)fg;
+                spec[sl + nsl * (gbin - 1)] = spec[sl + nsl * (gbin - 1)] + p->ch;
+            }
+            if (pass == 0)
+                for (int64_t l = 0; l < nsl; l++) {
+                    um[l] = um[l] / nd[l];
+                    vm[l] = vm[l] / nd[l];
+                    wm[l] = wm[l] / nd[l];
+                }
+        }
+    }
+    free(um);
+    *gmin_out = gammin;
+    *gmax_out = gammax;
+}

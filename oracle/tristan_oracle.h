@@ -206,6 +206,12 @@ void to_step_shock(to_state *s, to_shock *k);
    imomy imomz eener iener; num receives the moment, den the box-averaged
    weight (both mx*my*mz); the current arrays are left as they were */
 void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, float *den);
+/* flow-frame energy spectra per slice (save_spectrum_2d,
+   code/output.F90:794-1249); dims from to_spectrum_dims */
+float to_log10f(float x);
+int to_spectrum_dims(const to_state *s, int gambins, int *nx, int *ny);
+void to_spectrum_2d(const to_state *s, int gambins, float *spec_i, float *spec_e, float *xgamma, float *xslice,
+                    float *yslice, float *gmin_out, float *gmax_out);
 /* sin and cos of a float argument, evaluated in double and rounded once */
 void to_sincosf(float x, float *sn, float *cs);
 

@@ -13,6 +13,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include "tg_internal.cuh"
+#include "tg_spectrum.cuh"
 
 using namespace tg;
 
@@ -1447,5 +1448,70 @@ extern "C" int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, i
     CK(cudaMemcpyAsync(num, f3[0], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaMemcpyAsync(den, f3[1], lot * 4, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// flow-frame energy spectra (save_spectrum_2d, code/output.F90:794-1249)
+// ---------------------------------------------------------------------------
+extern "C" int tg_spectrum_dims(tg_ctx *ctx, int32_t gambins, int32_t *nxbins, int32_t *nybins) {
+    if (!ctx || !nxbins || !nybins || gambins < 1) return TG_ERR_ARG;
+    const SpecGrid sg = spec_grid(ctx->g.mx, ctx->g.my, ctx->g.ng, gambins);
+    *nxbins = sg.nxb;
+    *nybins = sg.nyb;
+    return TG_OK;
+}
+
+extern "C" int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *xgamma,
+                           float *xslice, float *yslice, float *gamma_range) {
+    if (!ctx || !spec_ions || !spec_lecs || !xgamma || !xslice || !yslice || gambins < 1) return TG_ERR_ARG;
+    const SpecGrid sg = spec_grid(ctx->g.mx, ctx->g.my, ctx->g.ng, gambins);
+    const long long nsl = (long long)sg.nxb * sg.nyb;
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    // scratch: 4 FP64 sums and 3 means per slice, the gamma range, the histogram
+    double *acc = nullptr;
+    float *mean = nullptr, *spec = nullptr;
+    unsigned *range = nullptr;
+    cudaError_t e = cudaMalloc(&acc, (size_t)nsl * 4 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&mean, (size_t)nsl * 3 * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&spec, (size_t)nsl * gambins * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&range, 8);
+    const unsigned one = 0x3f800000u;  // 1.0f
+    const unsigned init[2] = {one, one};
+    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, (size_t)nsl * 4 * 8, ctx->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(range, init, 8, cudaMemcpyHostToDevice, ctx->st);
+    if (e == cudaSuccess) e = launch_spec_range(ctx->sp[ctx->par], ctx->d_cnt + 2 * ctx->par, n[0] + n[1], range, ctx->st);
+    unsigned got[2] = {one, one};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(got, range, 8, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    float gmin, gmax;
+    memcpy(&gmin, &got[0], 4);
+    memcpy(&gmax, &got[1], 4);
+    const float gammin = fmaxf(gmin, 1.0f + 1e-6f);
+    const float lg0 = log10_single(gammin - 1.0f);
+    const float dgam = (log10_single(gmax - 1.0f) - lg0) / (float)gambins;
+    for (int i = 1; i <= gambins; i++) xgamma[i - 1] = powf(10.0f, (float)(i - 1) * dgam + lg0);
+    for (int i = 1; i <= sg.nxb; i++) xslice[i - 1] = sg.dxslice * (float)(i - 1) + 0.5f * sg.dxslice + (float)sg.mxmin;
+    for (int i = 1; i <= sg.nyb; i++) yslice[i - 1] = sg.dyslice * (float)(i - 1) + 0.5f * sg.dyslice + (float)sg.mymin;
+    if (gamma_range) {
+        gamma_range[0] = gammin;
+        gamma_range[1] = gmax;
+    }
+    for (int s = 0; s < 2 && e == cudaSuccess; s++) {
+        float *out = s == 0 ? spec_ions : spec_lecs;
+        e = cudaMemsetAsync(spec, 0, (size_t)nsl * gambins * 4, ctx->st);
+        if (e == cudaSuccess)
+            e = launch_spec_species(ctx->g, ctx->P, sg, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,
+                                    n[s], acc, mean, lg0, dgam, spec, ctx->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, spec, (size_t)nsl * gambins * 4, cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    }
+    cudaFree(acc);
+    cudaFree(mean);
+    cudaFree(spec);
+    cudaFree(range);
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_spectrum: %s", cudaGetErrorString(e));
     return check_status(ctx);
 }

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "tg_particles.cuh"
+#include "tg_spectrum.cuh"
 
 namespace tg {
 
@@ -305,6 +306,131 @@ cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, co
     if (e != cudaSuccess) return e;
     if ((e = launch_fold(g, P, f3, st)) != cudaSuccess) return e;
     k_moments_box<<<dgrid(g.lot), 256, 0, st>>>(g, kind, idx, idy, idz, f3[0], f3[1]);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// flow-frame energy spectra per slice (save_spectrum_2d,
+// code/output.F90:794-1249)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool spec_slice(const SpecGrid &sg, float x, float y, long long mxcum, long long mycum,
+                                           int &sl) {
+    const float fxb = (x + (float)mxcum - (float)sg.mxmin) / sg.dxslice + 1.0f;
+    const float fyb = (y + (float)mycum - (float)sg.mymin) / sg.dyslice + 1.0f;
+    if (!(fxb >= 1.0f && fyb >= 1.0f)) return false;
+    const int xb = (int)fxb, yb = (int)fyb;
+    if (xb > sg.nxb || yb > sg.nyb) return false;
+    sl = (xb - 1) + sg.nxb * (yb - 1);
+    return true;
+}
+
+// gamma range over every particle (starting from 1, as the reference)
+__global__ void __launch_bounds__(256) k_spec_range(Species si, Species se, const long long *count,
+                                                    unsigned *gmin, unsigned *gmax) {
+    const long long n0 = count[0], n1 = count[1];
+    float lo = 1.0f, hi = 1.0f;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n0 + n1;
+         t += (long long)gridDim.x * blockDim.x) {
+        const Species &sp = t < n0 ? si : se;
+        const long long n = t < n0 ? t : t - n0;
+        if (sp.cell[n] < 0) continue;
+        const float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+        const float gam = sqrtf(1.0f + (u * u + v * v + w * w));
+        lo = fminf(lo, gam);
+        hi = fmaxf(hi, gam);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {  // gamma >= 1 > 0: float order is integer order
+        atomicMin(gmin, __float_as_uint(lo));
+        atomicMax(gmax, __float_as_uint(hi));
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_spec_means(Geom g, Params P, SpecGrid sg, Species sp, const long long *count,
+                                                    double *acc) {
+    const long long nsl = (long long)sg.nxb * sg.nyb;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < *count;
+         n += (long long)gridDim.x * blockDim.x) {
+        if (sp.cell[n] < 0 || sp.ind[n] <= 0) continue;
+        float x, y, z;
+        load_pos<DIM>(g, sp, n, x, y, z);
+        int sl;
+        if (!spec_slice(sg, x, y, P.mxcum, P.mycum, sl)) continue;
+        const float u = sp.u[n], v = sp.v[n], w = sp.w[n], ch = sp.ch[n];
+        const float gam = sqrtf(1.0f + (u * u + v * v + w * w));
+        atomicAdd(acc + sl, (double)ch);
+        atomicAdd(acc + nsl + sl, (double)((u / gam) * ch));
+        atomicAdd(acc + 2 * nsl + sl, (double)((v / gam) * ch));
+        atomicAdd(acc + 3 * nsl + sl, (double)((w / gam) * ch));
+    }
+}
+
+// slice means: the sums rounded to single, divided as the reference does
+__global__ void k_spec_divide(long long nsl, double *acc, float *mean) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nsl;
+         t += (long long)gridDim.x * blockDim.x) {
+        const float nd = __double2float_rn(acc[t]);
+        for (int c = 0; c < 3; c++) mean[c * nsl + t] = __double2float_rn(acc[(c + 1) * nsl + t]) / nd;
+        for (int c = 0; c < 4; c++) acc[c * nsl + t] = 0.0;
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_spec_bins(Geom g, Params P, SpecGrid sg, Species sp, const long long *count,
+                                                   const float *mean, float lg0, float dgam, float *spec) {
+    const long long nsl = (long long)sg.nxb * sg.nyb;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < *count;
+         n += (long long)gridDim.x * blockDim.x) {
+        if (sp.cell[n] < 0 || sp.ind[n] <= 0) continue;
+        float x, y, z;
+        load_pos<DIM>(g, sp, n, x, y, z);
+        int sl;
+        if (!spec_slice(sg, x, y, P.mxcum, P.mycum, sl)) continue;
+        const float u = sp.u[n], v = sp.v[n], w = sp.w[n], ch = sp.ch[n];
+        const float gam = sqrtf(1.0f + (u * u + v * v + w * w));
+        const float vx = mean[sl], vy = mean[nsl + sl], vz = mean[2 * nsl + sl];
+        const float vr = sqrtf(vx * vx + vy * vy + vz * vz);
+        const float gvr = 1.0f / sqrtf(1.0f - vr * vr);
+        const float vr2 = vr * vr;
+        const float up = -vx * gvr * gam + (1.0f + (gvr - 1.0f) * (vx * vx) / vr2) * u +
+                         (gvr - 1.0f) * vx * vy / vr2 * v + (gvr - 1.0f) * vx * vz / vr2 * w;
+        const float vp = -vy * gvr * gam + (gvr - 1.0f) * vx * vy / vr2 * u +
+                         (1.0f + (gvr - 1.0f) * (vy * vy) / vr2) * v + (gvr - 1.0f) * vy * vz / vr2 * w;
+        const float wp = -vz * gvr * gam + (gvr - 1.0f) * vx * vz / vr2 * u +
+                         (gvr - 1.0f) * vy * vz / vr2 * v + (1.0f + (gvr - 1.0f) * (vz * vz) / vr2) * w;
+        const float gp = sqrtf(1.0f + (up * up + vp * vp + wp * wp));
+        const float fg = (log10_single(gp - 1.0f) - lg0) / dgam + 1.0f;
+        if (!(fg >= 1.0f && fg < (float)sg.gambins + 1.0f)) continue;
+        const int gbin = (int)fg;
+        atomicAdd(spec + sl + nsl * (gbin - 1), ch);
+    }
+}
+
+static int dgrid(long long n);
+
+cudaError_t launch_spec_range(const Species *sp, const long long *count, long long hint, unsigned *gminmax,
+                              cudaStream_t st) {
+    k_spec_range<<<dgrid(hint), 256, 0, st>>>(sp[0], sp[1], count, gminmax, gminmax + 1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &sg, const Species &sp,
+                                const long long *count, long long hint, double *acc, float *mean, float lg0,
+                                float dgam, float *spec, cudaStream_t st) {
+    const long long nsl = (long long)sg.nxb * sg.nyb;
+    if (g.dims == 3) {
+        k_spec_means<3><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, acc);
+        k_spec_divide<<<dgrid(nsl), 256, 0, st>>>(nsl, acc, mean);
+        k_spec_bins<3><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec);
+    } else {
+        k_spec_means<2><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, acc);
+        k_spec_divide<<<dgrid(nsl), 256, 0, st>>>(nsl, acc, mean);
+        k_spec_bins<2><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec);
+    }
     return cudaGetLastError();
 }
 

@@ -462,6 +462,14 @@ struct DiagLaunch {
     bool particles;  // false: the lap's tile kernel already summed the particles
 };
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
+// flow-frame spectra (save_spectrum_2d): the gamma range (two float bit
+// patterns, seeded with 1.0), then per species slice means and the histogram
+struct SpecGrid;
+cudaError_t launch_spec_range(const Species *sp, const long long *count, long long hint, unsigned *gminmax,
+                              cudaStream_t st);
+cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &sg, const Species &sp,
+                                const long long *count, long long hint, double *acc, float *mean, float lg0,
+                                float dgam, float *spec, cudaStream_t st);
 // grid moments (meanq_fld_cur) into f3[0] (moment) and f3[1] (weight);
 // num / den are zeroed FP64 scratch of g.lot cells, left zeroed
 cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,
