@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-shock", action="store_true")
     ap.add_argument("--shock-steps", type=int, default=100)
+    ap.add_argument("--shock-sort-every", type=int, default=4,
+                    help="tile sort cadence of the shock run (injected particles ride the tail kernel between sorts)")
     ap.add_argument("--ens-boxes", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=40)
     ap.add_argument("--ens-tile", type=int, nargs=2, default=None,
@@ -328,15 +330,16 @@ def run_shock(args, device):
     """The 2D pair shock on 8192 x 512 cells (order 3, 16 per cell per
     species upstream, gamma0 = 15, sigma = 0.1): the initial half-box load
     drawn on the device, then laps with the reflecting wall, conductor and
-    moving injector running as kernels inside the lap (graph-replayed, tile
-    sort every lap). particle-steps/s use the mean particle count of the
-    timed laps."""
+    moving injector running as kernels inside the lap (graph-replayed; the
+    particles injected between two tile sorts are moved by the tail kernel).
+    particle-steps/s use the mean particle count of the timed laps."""
     from tristan_gb300 import setups
     from tristan_gb300.gpu import GpuSim, SYNC_ALL
-    cfg = setups.make_config("shock2d_8192x512_o3", sort_every=1)
+    se = max(1, args.shock_sort_every)
+    cfg = setups.make_config("shock2d_8192x512_o3", sort_every=se)
     sh, fields, region = setups.shock_params(cfg)
-    K = max(2, args.shock_steps // 2 * 2)
-    warm = max(args.warmup, 4) // 2 * 2
+    K = max(2 * se, args.shock_steps // (2 * se) * (2 * se))
+    warm = max(2 * se, max(args.warmup, 4) // (2 * se) * (2 * se))
     cfg.maxhlf = setups.shock_capacity(cfg, K + warm, sh)
     g = GpuSim(cfg, device=device)
     g.set_fields(**fields)
@@ -361,7 +364,7 @@ def run_shock(args, device):
             "value": mean_n * K / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / K,
             "particles_initial_load": n_load, "particles_timed": [n0, n1],
             "device_load_s": t_load, "xinject2": st["xinject2"], "walloc": st["walloc"],
-            "kernels_per_step": kps, "deposit": "fp32-atomic", "sort_every": 1,
+            "kernels_per_step": kps, "deposit": "fp32-atomic", "sort_every": se,
             "hooks": "reflecting wall + zigzag, conductor, moving injector (jump-ahead Park-Miller)"}
 
 

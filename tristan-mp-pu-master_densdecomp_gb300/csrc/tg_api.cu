@@ -814,8 +814,10 @@ static long long host_powmod31(long long a, long long e) {
 extern "C" int tg_shock_init(tg_ctx *ctx, const tg_shock *k) {
     if (!ctx || !k) return TG_ERR_ARG;
     if (ctx->g.dims != 2) return fail(ctx, TG_ERR_ARG, "tg_shock_init: the shock hooks are 2D");
-    if (ctx->cfg.sort_every > 1)
-        return fail(ctx, TG_ERR_ARG, "tg_shock_init: injection needs a tile sort every lap (sort_every = 1)");
+    // between sorts the injected particles sit past the tile ranges: the tail
+    // kernel moves them, but the tile-wise diagnostics pass would miss them
+    if (ctx->cfg.sort_every > 1 && ctx->cfg.diag_every > 0)
+        return fail(ctx, TG_ERR_ARG, "tg_shock_init: per-lap diagnostics with injection need sort_every = 1");
     if (k->dseed < 1.0 || k->dseed >= 2147483647.0 || k->dseed != floor(k->dseed))
         return fail(ctx, TG_ERR_ARG, "tg_shock_init: dseed must be an integer in [1, 2^31 - 2]");
     std::vector<float> tab(4 * (TG_PDF_SZ + 1));
@@ -997,6 +999,10 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
     // push and the deposit; the wall advances first
     if (ctx->shock_on && ctx->K.wall) { CK(launch_wall_step(ctx->P, ctx->K, ctx->d_shock, st)); k++; }
     CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++;
+    if (ctx->shock_on && ctx->cfg.sort_every > 1) {
+        // the particles injected since the last sort
+        CK(launch_tail(a, ctx->d_cnt + 2 * ctx->par, ctx->P.fixed != 0, st)); k++;
+    }
     CK(mark(ctx, li, 1, 1));
     CK(mark(ctx, li, 2, 0));
     // advance_Bhalfstep; bc_b1; bc_b2 (:139-145); [field_bc_user];
@@ -1172,6 +1178,8 @@ extern "C" int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases) {
 
 extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
     if (!ctx || !out) return TG_ERR_ARG;
+    // injected particles may sit past the tile ranges since the last sort
+    if (ctx->shock_on && ctx->cfg.sort_every > 1) ctx->dirty = true;
     int r = ensure_sorted(ctx);
     if (r) return r;
     if ((r = run_diag(ctx, true))) return r;

@@ -35,8 +35,11 @@ struct DiagArgs {
     int *status;
 };
 
+#ifndef TG_DIAG_MINB
+#define TG_DIAG_MINB 4
+#endif
 template <int DIM, int ORDER>
-__global__ void __launch_bounds__(256, 4) k_diag_particles(DiagArgs a) {
+__global__ void __launch_bounds__(256, TG_DIAG_MINB) k_diag_particles(DiagArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
     int *winhi = reinterpret_cast<int *>(smem_raw) + a.g.wcells;

@@ -418,6 +418,8 @@ struct TileArgs {
 // launchers (tg_particles.cu)
 // ---------------------------------------------------------------------------
 cudaError_t launch_tiles(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st);
+// the lap of the particles appended since the last tile sort (2D; injection)
+cudaError_t launch_tail(const TileArgs &a, const long long *count, bool fixed, cudaStream_t st);
 cudaError_t launch_push_flat(const Geom &g, const Params &P, const FieldPtrs &f, const Species &sp,
                              const long long *dcount, long long count, float qm, int *status, cudaStream_t st);
 cudaError_t launch_tile_count(const Geom &g, const Species &sp, const long long *count, long long hint, int *hist,

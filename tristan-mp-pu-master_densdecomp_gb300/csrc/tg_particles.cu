@@ -11,6 +11,9 @@ extern template cudaError_t launch_tiles_o<2, 3>(const TileArgs &, bool, bool, b
 extern template cudaError_t launch_tiles_o<3, 1>(const TileArgs &, bool, bool, bool, cudaStream_t, size_t);
 extern template cudaError_t launch_tiles_o<3, 2>(const TileArgs &, bool, bool, bool, cudaStream_t, size_t);
 extern template cudaError_t launch_tiles_o<3, 3>(const TileArgs &, bool, bool, bool, cudaStream_t, size_t);
+extern template cudaError_t launch_tail_o<2, 1>(const TileArgs &, const long long *, bool, cudaStream_t);
+extern template cudaError_t launch_tail_o<2, 2>(const TileArgs &, const long long *, bool, cudaStream_t);
+extern template cudaError_t launch_tail_o<2, 3>(const TileArgs &, const long long *, bool, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // tile counting sort
@@ -220,6 +223,13 @@ cudaError_t launch_tiles(const TileArgs &a, bool fixed, bool push, bool deposit,
     if (d == 3 && o == 1) return launch_tiles_o<3, 1>(a, fixed, push, deposit, st, smem);
     if (d == 3 && o == 2) return launch_tiles_o<3, 2>(a, fixed, push, deposit, st, smem);
     return launch_tiles_o<3, 3>(a, fixed, push, deposit, st, smem);
+}
+
+cudaError_t launch_tail(const TileArgs &a, const long long *count, bool fixed, cudaStream_t st) {
+    if (a.g.dims != 2) return cudaErrorInvalidValue;  // injection is 2D only
+    if (a.g.order == 1) return launch_tail_o<2, 1>(a, count, fixed, st);
+    if (a.g.order == 2) return launch_tail_o<2, 2>(a, count, fixed, st);
+    return launch_tail_o<2, 3>(a, count, fixed, st);
 }
 
 cudaError_t launch_push_flat(const Geom &g, const Params &P, const FieldPtrs &f, const Species &sp,

@@ -522,6 +522,63 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
 #define TG_TILE_THREADS_3D 256
 #endif
 #define TG_TILE_THREADS(DIM) ((DIM) == 3 ? TG_TILE_THREADS_3D : 256)
+// One particle's lap inside the tile kernel (and the tail kernel): push,
+// [wall], Esirkepov deposit into the sink, wrap or discard, store, count
+// its new tile.
+template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
+__device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXED> &sink, const Species &sp, int n,
+                                              int *newcount, float qm, float qs, double walloc, double x2in) {
+    const Geom &g = a.g;
+            if (sp.cell[n] < 0) return;  // discarded since the last sort
+            float x, y, z;
+            load_pos<DIM>(g, sp, n, x, y, z);
+            float u = sp.u[n], v = sp.v[n], w = sp.w[n];
+            if (PUSH) {
+                if (!gather_safe<DIM>(g, x, y, z)) {
+                    atomicOr(a.status, ST_BOUNDS);
+                    sp.cell[n] = -1;
+                    return;
+                }
+                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
+                if (DIM == 2 && DEPOSIT && (double)(x + (float)a.P.mxcum) < walloc &&
+                    !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
+                                  y, z, u, v, w)) {
+                    sp.cell[n] = -1;  // removed by the wall (dropped by the next sort)
+                    if (a.dead) *a.dead = 1;
+                    return;
+                }
+            }
+            bool keep = true;
+            if (DEPOSIT) {
+                // reconstruct the previous position from the new momentum
+                // (deposit_particles, code/particles_movedeposit.F90:1384-1390)
+                const float c = a.P.c;
+                const float invgam = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
+                const float x0 = x - u * invgam * c;
+                const float y0 = y - v * invgam * c;
+                const float z0 = z - w * invgam * c;
+                const float q = sp.ch[n] * qs;
+                esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
+                keep = wrap_particle<DIM>(g, a.P, x, y, z, x2in);
+            }
+            int i, j, k;
+            const bool fin = isfinite(x) && isfinite(y) && isfinite(z);
+            if (!fin) atomicOr(a.status, ST_NAN);
+            if (keep && fin && pos_cell<DIM>(g, x, y, z, i, j, k)) {
+                store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
+                if (newcount) agg_inc(newcount, tile_of(g, i, j, k));
+            } else {
+                if (keep) atomicOr(a.status, ST_BOUNDS);
+                else if (a.dead) *a.dead = 1;
+                sp.cell[n] = -1;  // discarded: dropped by the next sort
+            }
+            if (PUSH) {
+                sp.u[n] = u;
+                sp.v[n] = v;
+                sp.w[n] = w;
+            }
+}
+
 // One tile: push, deposit into the shared window, wrap, flush. Every thread
 // of the CTA calls it with the same tile (it contains barriers); smem_raw is
 // the 6 * wcells words of the window.
@@ -571,56 +628,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
         for (int b0 = beg; b0 < end;) {
             const int b1 = min(end, b0 + (TG_WIN_BATCH - since));
 #pragma unroll 1
-            for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x) {
-                if (sp.cell[n] < 0) continue;  // discarded since the last sort
-                float x, y, z;
-                load_pos<DIM>(g, sp, n, x, y, z);
-                float u = sp.u[n], v = sp.v[n], w = sp.w[n];
-                if (PUSH) {
-                    if (!gather_safe<DIM>(g, x, y, z)) {
-                        atomicOr(a.status, ST_BOUNDS);
-                        sp.cell[n] = -1;
-                        continue;
-                    }
-                    push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
-                    if (DIM == 2 && DEPOSIT && (double)(x + (float)a.P.mxcum) < walloc &&
-                        !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
-                                      y, z, u, v, w)) {
-                        sp.cell[n] = -1;  // removed by the wall (dropped by the next sort)
-                        if (a.dead) *a.dead = 1;
-                        continue;
-                    }
-                }
-                bool keep = true;
-                if (DEPOSIT) {
-                    // reconstruct the previous position from the new momentum
-                    // (deposit_particles, code/particles_movedeposit.F90:1384-1390)
-                    const float c = a.P.c;
-                    const float invgam = 1.0f / sqrtf(1.0f + u * u + v * v + w * w);
-                    const float x0 = x - u * invgam * c;
-                    const float y0 = y - v * invgam * c;
-                    const float z0 = z - w * invgam * c;
-                    const float q = sp.ch[n] * qs;
-                    esirkepov<DIM, ORDER>(g, x, y, z, x0, y0, z0, q, sink, a.status);
-                    keep = wrap_particle<DIM>(g, a.P, x, y, z, x2in);
-                }
-                int i, j, k;
-                const bool fin = isfinite(x) && isfinite(y) && isfinite(z);
-                if (!fin) atomicOr(a.status, ST_NAN);
-                if (keep && fin && pos_cell<DIM>(g, x, y, z, i, j, k)) {
-                    store_pos<DIM>(g, sp, n, x, y, z, i, j, k);
-                    if (a.newcount[s]) agg_inc(a.newcount[s], tile_of(g, i, j, k));
-                } else {
-                    if (keep) atomicOr(a.status, ST_BOUNDS);
-                    else if (a.dead) *a.dead = 1;
-                    sp.cell[n] = -1;  // discarded: dropped by the next sort
-                }
-                if (PUSH) {
-                    sp.u[n] = u;
-                    sp.v[n] = v;
-                    sp.w[n] = w;
-                }
-            }
+            for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x)
+                particle_step<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, sink, sp, n, a.newcount[s], qm, qs, walloc, x2in);
             since += b1 - b0;
             b0 = b1;
             if (DEPOSIT && since == TG_WIN_BATCH) {
@@ -644,6 +653,38 @@ __global__ void __launch_bounds__(TG_TILE_THREADS(DIM), DIM == 3 ? TG_TILES_MINB
     k_tiles(TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     tile_body<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, blockIdx.x, smem_raw);
+}
+
+// Particles appended after the last tile sort (the injector's, between
+// sorts) live past tstart[s][ntiles] and belong to no tile range: the same
+// lap as in the tile kernel, with an empty window so that every deposit goes
+// to global memory. count = the live count of each species on the device.
+template <int DIM, int ORDER, bool FIXED>
+__global__ void __launch_bounds__(256) k_tail(TileArgs a, const long long *count) {
+    WindowSink<FIXED> sink;
+    sink.lo = nullptr;
+    sink.hi = nullptr;
+    sink.wx0 = sink.wy0 = sink.wz0 = 0;
+    sink.wx = sink.wy = sink.wz = 0;  // fits() and add() never take the window
+    sink.wcells = 0;
+    for (int cc = 0; cc < 3; cc++) {
+        sink.gc[cc] = a.cur[cc];
+        sink.gf[cc] = a.fix[cc];
+    }
+    sink.scale = a.P.fx_scale;
+    sink.g = &a.g;
+    sink.status = a.status;
+    const double walloc = (a.shock && a.wall) ? a.shock->walloc : -1.0e300;
+    const double x2in = a.shock ? a.shock->x2in : a.P.x2in;
+#pragma unroll 1
+    for (int s = 0; s < 2; s++) {
+        const long long beg = a.tstart[s][a.g.ntiles], end = count[s];
+        const float qm = a.P.qm[s], qs = a.P.qs[s];
+        for (long long n = beg + blockIdx.x * (long long)blockDim.x + threadIdx.x; n < end;
+             n += (long long)gridDim.x * blockDim.x)
+            particle_step<DIM, ORDER, FIXED, true, true>(a, sink, a.sp[s], (int)n, a.newcount[s], qm, qs, walloc,
+                                                         x2in);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -708,4 +749,13 @@ cudaError_t launch_tiles_o(const TileArgs &a, bool fixed, bool push, bool deposi
 
 template <int DIM, int ORDER>
 cudaError_t launch_tiles_o(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st, size_t smem);
+
+// k_tail over a fixed grid (the tail is a few laps of injection at most)
+template <int DIM, int ORDER>
+cudaError_t launch_tail_o(const TileArgs &a, const long long *count, bool fixed, cudaStream_t st) {
+    const int grid = 2 * 152;
+    if (fixed) k_tail<DIM, ORDER, true><<<grid, 256, 0, st>>>(a, count);
+    else k_tail<DIM, ORDER, false><<<grid, 256, 0, st>>>(a, count);
+    return cudaGetLastError();
+}
 }  // namespace tg

@@ -3,4 +3,5 @@
 
 namespace tg {
 template cudaError_t launch_tiles_o<2, 3>(const TileArgs &, bool, bool, bool, cudaStream_t, size_t);
+template cudaError_t launch_tail_o<2, 3>(const TileArgs &, const long long *, bool, cudaStream_t);
 }  // namespace tg
