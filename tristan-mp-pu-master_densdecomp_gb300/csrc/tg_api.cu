@@ -187,10 +187,18 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.nty = (ny + ty - 1) / ty;
     g.ntz = c.dims == 3 ? (nz + tz - 1) / tz : 1;
     g.ntiles = g.ntx * g.nty * g.ntz;
+    // The deposit stencil of a particle whose lap starts in cell i spans
+    // cells [i - 2, i + 3] (shape orders 2 and 3; [i - 1, i + 2] for order
+    // 1). A sort leaves every particle in its tile, and between sorts a
+    // particle moves less than c cells per lap, so the window covers the
+    // tile, the stencil and the drift of the laps since the last sort.
     const int se = c.sort_every < 1 ? 1 : c.sort_every;
-    const int drift = 1 + (int)ceilf((float)(se - 1) * c.c);
-    g.wlo = 2 + drift;
-    g.whi = 3 + drift;
+#ifndef TG_HALO_EXTRA
+#define TG_HALO_EXTRA 0
+#endif
+    const int drift = TG_HALO_EXTRA + (int)ceilf((float)(se - 1) * c.c);
+    g.wlo = (c.order == 1 ? 1 : 2) + drift;
+    g.whi = (c.order == 1 ? 2 : 3) + drift;
     g.wx = tx + g.wlo + g.whi;
     g.wy = ty + g.wlo + g.whi;
     g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
