@@ -160,6 +160,16 @@ int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force);
    inject_particles_user at their places), fused and replayed from a
    captured CUDA graph. */
 int tg_step(tg_ctx *ctx, int32_t nsteps);
+/* nsteps passes of the main loop (code/tristanmainloop.F90:115-303) with the
+   bound host arrays as the state of record, as when the reference's loop
+   keeps its own arrays between laps: per lap E, B and the particle records
+   (tg_bind_fields / tg_bind_particles) go to the device, the lap runs, and
+   E, B, the currents, the records and the counts come back before the call
+   returns. With page-locked host records on an all-periodic domain the
+   record transfers of one species overlap the other species' sort and push
+   and the field phases; otherwise it is tg_sync_from_host + tg_step(1) +
+   tg_sync_to_host per lap. */
+int tg_step_host(tg_ctx *ctx, int32_t nsteps);
 /* tg_step bracketed by CUDA events on the context's stream; *ms receives
    the device time of the nsteps laps. Synchronises. */
 int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms);

@@ -78,6 +78,12 @@ struct tg_ctx {
     tg_shock hshock;
     // grid-moment scratch (FP64 sums)
     double *mom[2] = {};
+    // host-driven laps (tg_step_host): copy streams, events, staging copy of
+    // the host records (both species)
+    cudaStream_t st_up = nullptr, st_down = nullptr;
+    cudaEvent_t ev_link[5] = {};
+    void *stage2 = nullptr;
+    long long host_n[2] = {0, 0};
     char err[512] = {0};
     std::vector<void *> allocs;
 };
@@ -343,9 +349,14 @@ extern "C" void tg_finalize(tg_ctx *ctx) {
     for (auto &e : ctx->ev) cudaEventDestroy(e);
     for (void *q : ctx->allocs) cudaFree(q);
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->stage2) cudaFree(ctx->stage2);
     for (int a = 0; a < 4; a++)
         if (ctx->rk[a]) cudaFree(ctx->rk[a]);
     if (ctx->cub_tmp) cudaFree(ctx->cub_tmp);
+    for (auto &e : ctx->ev_link)
+        if (e) cudaEventDestroy(e);
+    if (ctx->st_up) cudaStreamDestroy(ctx->st_up);
+    if (ctx->st_down) cudaStreamDestroy(ctx->st_down);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -984,7 +995,21 @@ static cudaError_t mark(tg_ctx *ctx, int li, int phase, int end) {
     return cudaEventRecord(ctx->ev[((size_t)li * TG_NPHASES + phase) * 2 + end], ctx->st);
 }
 
-static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
+// The overlapped host-driven lap (tg_step_host): the records of each species
+// travel by DMA (copy engines, no SMs) between the page-locked host array and
+// a device staging copy of it; each species is converted and sorted as soon
+// as its records are in, pushed by its own tile launch, converted back and
+// sent home while the other species and the field phases run.
+struct HostPipe {
+    char *host;             // the bound host records
+    char *stage;            // device staging copy, same layout
+    cudaStream_t down;      // device -> host copies
+    cudaEvent_t uploaded[2], pushed[2];
+};
+
+static int sort_species(tg_ctx *ctx, int s, bool counted);
+
+static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const HostPipe *pipe = nullptr) {
     cudaStream_t st = ctx->st;
     const Geom &g = ctx->g;
     int k = 0;
@@ -1002,11 +1027,39 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
         for (int a = 6; a < 9; a++) CK(cudaMemsetAsync(ctx->f[a], 0, (size_t)g.lot * 4, st));
     CK(mark(ctx, li, 0, 1));
     CK(mark(ctx, li, 1, 0));
+    if (pipe) {
+        // species by species: the freshly uploaded records into the particle
+        // arrays, the tile sort (into the other parity), the push, and the
+        // records back to the staging copy, from where they go home
+        const int p0 = ctx->par;
+        CK(cudaMemsetAsync(ctx->d_dead, 0, sizeof(int), st));  // the sorts compact
+        ctx->fault_seen = false;
+        for (int s = 0; s < 2; s++) {
+            const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+            CK(cudaStreamWaitEvent(st, pipe->uploaded[s], 0));
+            CK(launch_aos_to_soa(g, pipe->stage + off, ctx->sp[p0][s], ctx->host_n[s], ctx->d_status, st));
+            int rr = sort_species(ctx, s, false);
+            if (rr) return rr;
+            TileArgs a = tile_args(ctx, false);
+            a.sp[s] = ctx->sp[1 - p0][s];  // this species is sorted already
+            a.only = s + 1;
+            CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st));
+            CK(launch_soa_to_aos(g, ctx->sp[1 - p0][s], pipe->stage + off, ctx->host_n[s], st));
+            CK(cudaEventRecord(pipe->pushed[s], st));
+            CK(cudaStreamWaitEvent(pipe->down, pipe->pushed[s], 0));
+            CK(cudaMemcpyAsync(pipe->host + off, pipe->stage + off, (size_t)ctx->host_n[s] * AOS,
+                               cudaMemcpyDeviceToHost, pipe->down));
+            k += 6;
+        }
+        ctx->par = 1 - p0;
+        ctx->dirty = false;
+        ctx->may_have_dead = false;
+    }
     TileArgs a = tile_args(ctx, sort_now);
     // particle_bc_user (the wall) runs inside the tile kernel, between the
     // push and the deposit; the wall advances first
     if (ctx->shock_on && ctx->K.wall) { CK(launch_wall_step(ctx->P, ctx->K, ctx->d_shock, st)); k++; }
-    CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++;
+    if (!pipe) { CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st)); k++; }
     if (ctx->shock_on && ctx->cfg.sort_every > 1) {
         // the particles injected since the last sort
         CK(launch_tail(a, ctx->d_cnt + 2 * ctx->par, ctx->P.fixed != 0, st)); k++;
@@ -1043,7 +1096,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0) {
         k += 4;
     }
     CK(mark(ctx, li, 3, 1));
-    if (sort_now) {
+    if (sort_now && !pipe) {
         CK(mark(ctx, li, 4, 0));
         int rr = sort_all(ctx, true);
         if (rr) return rr;
@@ -1139,6 +1192,98 @@ extern "C" int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms) {
     cudaEventDestroy(b);
     if (r) return r;
     return check_status(ctx);
+}
+
+// One main-loop pass with the bound host arrays as the state: E, B and the
+// particle records go up, the lap runs, every field and record comes back.
+// With page-locked host records on an all-periodic domain (no particle can
+// leave) the transfers overlap the lap species by species; otherwise the
+// same steps run one after another.
+static int host_lap(tg_ctx *ctx) {
+    const Geom &g = ctx->g;
+    const bool periodic = g.per[0] && g.per[1] && (g.dims == 2 || g.per[2]);
+    bool bound = ctx->hp != nullptr;
+    for (int a = 0; a < 9; a++) bound = bound && ctx->hf[a] != nullptr;
+    // page-locked records (the copies are then asynchronous DMA)
+    const bool locked = bound && host_view(ctx, ctx->hp) != nullptr;
+    if (!(locked && periodic && !ctx->shock_on)) {
+        int r = tg_sync_from_host(ctx, TG_SYNC_E | TG_SYNC_B | TG_SYNC_PARTICLES);
+        if (!r) r = tg_step(ctx, 1);
+        if (!r) r = tg_sync_to_host(ctx, TG_SYNC_ALL);
+        return r;
+    }
+    const long long n[2] = {*ctx->hions, *ctx->hlecs};
+    for (int s = 0; s < 2; s++)
+        if (n[s] < 0 || n[s] > ctx->cfg.maxhlf)
+            return fail(ctx, TG_ERR_OVERFLOW, "species %d count %lld outside [0, maxhlf=%lld]", s, n[s],
+                        (long long)ctx->cfg.maxhlf);
+    if (!ctx->st_up) {
+        CK(cudaStreamCreateWithFlags(&ctx->st_up, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&ctx->st_down, cudaStreamNonBlocking));
+        for (auto &e : ctx->ev_link) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (!ctx->stage2) CK(cudaMalloc(&ctx->stage2, (size_t)ctx->cfg.maxhlf * AOS * 2 + 256));
+    HostPipe pipe;
+    pipe.host = (char *)ctx->hp;
+    pipe.stage = (char *)ctx->stage2;
+    pipe.down = ctx->st_down;
+    pipe.uploaded[0] = ctx->ev_link[0];
+    pipe.uploaded[1] = ctx->ev_link[1];
+    pipe.pushed[0] = ctx->ev_link[2];
+    pipe.pushed[1] = ctx->ev_link[3];
+    cudaStream_t st = ctx->st;
+    const size_t lot = (size_t)g.lot;
+    CK(cudaStreamSynchronize(st));
+    for (int s = 0; s < 2; s++) {
+        ctx->host_n[s] = n[s];
+        ctx->hcount[s] = n[s];
+        CK(cudaMemcpyAsync(ctx->d_cnt + 2 * ctx->par + s, &ctx->host_n[s], sizeof(long long),
+                           cudaMemcpyHostToDevice, st));
+    }
+    // E and B first: host-to-device copies leave in the order they are
+    // issued, and the lap's first phases need the fields only
+    for (int a = 0; a < 6; a++) CK(cudaMemcpyAsync(ctx->f[a], ctx->hf[a], lot * 4, cudaMemcpyHostToDevice, st));
+    // the records go up by DMA once earlier work on the stream is done
+    CK(cudaEventRecord(ctx->ev_link[4], st));
+    CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_link[4], 0));
+    for (int s = 0; s < 2; s++) {
+        const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+        CK(cudaMemcpyAsync(pipe.stage + off, pipe.host + off, (size_t)n[s] * AOS, cudaMemcpyHostToDevice,
+                           ctx->st_up));
+        CK(cudaEventRecord(pipe.uploaded[s], ctx->st_up));
+    }
+    int nk = 0;
+    int r = lap_kernels(ctx, false, &nk, 1 << 20, &pipe);
+    if (r) return r;
+    ctx->kernels_per_step = nk;
+    ctx->last_laps = 1;
+    ctx->last_direct = true;
+    ctx->lap += 1;
+    for (int a = 0; a < 9; a++) CK(cudaMemcpyAsync(ctx->hf[a], ctx->f[a], lot * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(ctx->ev_link[4], ctx->st_down));
+    CK(cudaStreamWaitEvent(st, ctx->ev_link[4], 0));
+    int flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(&flags[0], ctx->d_dead, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&flags[1], ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (flags[0] || flags[1]) {
+        // a record was dropped (outside the grid on the way up, or a fault):
+        // send the compacted records instead, and report the fault
+        ctx->may_have_dead = true;
+        return tg_sync_to_host(ctx, TG_SYNC_PARTICLES);
+    }
+    *ctx->hions = (int32_t)n[0];
+    *ctx->hlecs = (int32_t)n[1];
+    return TG_OK;
+}
+
+extern "C" int tg_step_host(tg_ctx *ctx, int32_t nsteps) {
+    if (!ctx || nsteps < 0) return TG_ERR_ARG;
+    for (int l = 0; l < nsteps; l++) {
+        int r = host_lap(ctx);
+        if (r) return r;
+    }
+    return TG_OK;
 }
 
 extern "C" int tg_enable_timing(tg_ctx *ctx, int32_t on) {

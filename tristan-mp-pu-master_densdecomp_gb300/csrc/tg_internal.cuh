@@ -412,6 +412,8 @@ struct TileArgs {
     // set to 1 when a particle is dropped on purpose (open boundary, wall),
     // so the host knows the next download must compact (null: not tracked)
     int *dead;
+    // species of this launch: 0 both, 1 ions only, 2 electrons only
+    int only;
 };
 
 // ---------------------------------------------------------------------------

@@ -619,7 +619,7 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     // across the CTA, so the barriers below are reached by all threads)
     int since = 0;
 #pragma unroll 1
-    for (int s = 0; s < 2; s++) {
+    for (int s = a.only == 2 ? 1 : 0; s < (a.only == 1 ? 1 : 2); s++) {
         const Species sp = a.sp[s];
         const int beg = a.tstart[s][tile], end = a.tstart[s][tile + 1];
         const float qm = a.P.qm[s];
