@@ -1107,7 +1107,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
         CK(mark(ctx, li, 5, 0));
         int rr = run_diag(ctx, true);
         if (rr) return rr;
-        k += 4 + ctx->cfg.ntimes;
+        k += 4 + ctx->g.dims * ctx->cfg.ntimes;
         CK(mark(ctx, li, 5, 1));
     }
     *nk = k;

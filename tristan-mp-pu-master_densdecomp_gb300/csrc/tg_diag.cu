@@ -10,7 +10,8 @@
 //                    (gamma-1 = u^2/(gamma+1) in FP32) and momentum summed
 //                    in FP64;
 //  k_rho_to_double   fixed point -> FP64 on the periodic interior;
-//  k_filter64        one FP64 binomial pass on the periodic interior;
+//  k_filter64_axis   one FP64 binomial pass on the periodic interior, as
+//                    [1, 2, 1] / 4 along each axis in turn;
 //  k_diag_fields     FP64 reductions: |div E - F(rho)|^2, |F(rho)|^2, total
 //                    charge, field energies and E x B momentum;
 //  k_diag_finish     writes the lap's record into the history ring.
@@ -116,37 +117,43 @@ __global__ void k_rho_to_double(long long n, double inv, unsigned long long *fx,
     }
 }
 
-// one binomial pass on the periodic interior (nx, ny, nz)
-template <int DIM>
-__global__ void k_filter64(int nx, int ny, int nz, const double *__restrict__ in, double *out) {
-    const long long n = (long long)nx * ny * nz;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % nx);
-        const long long r = t / nx;
-        const int j = (int)(r % ny), k = (int)(r / ny);
-        const int im = i == 0 ? nx - 1 : i - 1, ip = i == nx - 1 ? 0 : i + 1;
-        const int jm = j == 0 ? ny - 1 : j - 1, jp = j == ny - 1 ? 0 : j + 1;
-        double acc = 0.0;
-        if (DIM == 2) {
-            const double *row = in + (long long)j * nx, *rm = in + (long long)jm * nx, *rp = in + (long long)jp * nx;
-            acc = 4.0 * row[i] + 2.0 * (row[im] + row[ip] + rm[i] + rp[i]) + (rm[im] + rm[ip] + rp[im] + rp[ip]);
-            out[t] = acc * 0.0625;
-        } else {
-            const int km = k == 0 ? nz - 1 : k - 1, kp = k == nz - 1 ? 0 : k + 1;
-            const int ks[3] = {km, k, kp};
-            const double wk[3] = {1.0, 2.0, 1.0};
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const long long pl = (long long)ks[c] * ny;
-                const double *row = in + (pl + j) * nx, *rm = in + (pl + jm) * nx, *rp = in + (pl + jp) * nx;
-                acc += wk[c] * (4.0 * row[i] + 2.0 * (row[im] + row[ip] + rm[i] + rp[i]) +
-                                (rm[im] + rm[ip] + rp[im] + rp[ip]));
+// One binomial pass on the periodic interior (nx, ny, nz) is the product of
+// [1, 2, 1] / 4 along each axis; this is the pass along one axis. Weights
+// are powers of two, so every product and partial sum is exact while the
+// values keep below 2^53 units of the fixed-point grid they come from
+// (their order then does not matter). Rows (one y, z) are spread over the
+// blocks, cells of a row over the threads: no 64-bit index divisions.
+template <int AXIS>
+__global__ void __launch_bounds__(256) k_filter64_axis(int nx, int ny, int nz, const double *__restrict__ in,
+                                                       double *__restrict__ out) {
+    const int rows = ny * nz;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int j = row % ny, k = row / ny;
+        const long long base = (long long)row * nx;
+        long long om = 0, op = 0;  // row offsets of the neighbours (axes 1, 2)
+        if (AXIS == 1) {
+            om = (long long)((j == 0 ? ny - 1 : j - 1) + k * ny) * nx - base;
+            op = (long long)((j == ny - 1 ? 0 : j + 1) + k * ny) * nx - base;
+        } else if (AXIS == 2) {
+            om = (long long)(j + (k == 0 ? nz - 1 : k - 1) * ny) * nx - base;
+            op = (long long)(j + (k == nz - 1 ? 0 : k + 1) * ny) * nx - base;
+        }
+        for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+            const long long t = base + i;
+            double lo, hi;
+            if (AXIS == 0) {
+                lo = in[base + (i == 0 ? nx - 1 : i - 1)];
+                hi = in[base + (i == nx - 1 ? 0 : i + 1)];
+            } else {
+                lo = in[t + om];
+                hi = in[t + op];
             }
-            out[t] = acc * 0.015625;
+            out[t] = (2.0 * in[t] + (lo + hi)) * 0.25;
         }
     }
 }
+
+static int rgrid(int rows) { return rows < 152 * 16 ? (rows < 1 ? 1 : rows) : 152 * 16; }
 
 template <int DIM>
 __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__restrict__ ex, const float *__restrict__ ey,
@@ -155,13 +162,12 @@ __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__rest
                                                      const double *__restrict__ rho, double *acc) {
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
     const int lo = g.ng / 2 + 1, loz = DIM == 3 ? g.ngz / 2 + 1 : 1;
-    const long long n = (long long)nx * ny * nz;
     double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // res2 rho2 charge eE eB fx fy fz
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int a = (int)(t % nx);
-        const long long r = t / nx;
-        const int b = (int)(r % ny), c = (int)(r / ny);
+    // rows (one y, z) over the blocks, cells of a row over the threads
+    for (int row = blockIdx.x; row < ny * nz; row += gridDim.x)
+    for (int a = threadIdx.x; a < nx; a += blockDim.x) {
+        const long long t = (long long)row * nx + a;
+        const int b = row % ny, c = row / ny;
         const int i = lo + a, j = lo + b, k = loz + c;
         const long long l = lin(g, i, j, k);
         const int im = a == 0 ? lo + nx - 1 : i - 1, jm = b == 0 ? lo + ny - 1 : j - 1;
@@ -479,17 +485,21 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
     const long long n = (long long)nx * ny * nz;
     k_rho_to_double<<<dgrid(n), 256, 0, st>>>(n, d.P.fx_inv, d.rhofx, d.rho[0]);
     double *cur = d.rho[0], *nxt = d.rho[1];
+    const int rg = rgrid(ny * nz);
     for (int p = 0; p < d.ntimes; p++) {
-        if (g.dims == 3) k_filter64<3><<<dgrid(n), 256, 0, st>>>(nx, ny, nz, cur, nxt);
-        else k_filter64<2><<<dgrid(n), 256, 0, st>>>(nx, ny, nz, cur, nxt);
-        double *t = cur;
-        cur = nxt;
-        nxt = t;
+        for (int ax = 0; ax < g.dims; ax++) {
+            if (ax == 0) k_filter64_axis<0><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
+            else if (ax == 1) k_filter64_axis<1><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
+            else k_filter64_axis<2><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
+            double *t = cur;
+            cur = nxt;
+            nxt = t;
+        }
     }
     if (g.dims == 3)
-        k_diag_fields<3><<<dgrid(n), 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+        k_diag_fields<3><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
     else
-        k_diag_fields<2><<<dgrid(n), 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+        k_diag_fields<2><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
     k_diag_finish<<<1, 32, 0, st>>>(d.acc, d.hist, d.hist_cap, d.counter);
     return cudaGetLastError();
 }
