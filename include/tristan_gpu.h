@@ -170,6 +170,11 @@ int tg_step(tg_ctx *ctx, int32_t nsteps);
    and the field phases; otherwise it is tg_sync_from_host + tg_step(1) +
    tg_sync_to_host per lap. */
 int tg_step_host(tg_ctx *ctx, int32_t nsteps);
+/* Page-lock the bound host arrays (the nine fields and 2 * maxhlf particle
+   records) so host transfers run as asynchronous DMA; arrays already
+   page-locked are left as they are. Undone by tg_finalize. No counterpart
+   in the reference. */
+int tg_pin_host(tg_ctx *ctx);
 /* tg_step bracketed by CUDA events on the context's stream; *ms receives
    the device time of the nsteps laps. Synchronises. */
 int tg_step_timed(tg_ctx *ctx, int32_t nsteps, float *ms);

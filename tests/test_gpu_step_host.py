@@ -97,3 +97,22 @@ def test_step_host_drops_record_outside_grid():
     assert -50.0 not in set(g.ions["x"].tolist())
     g.step_host(1)  # the status word was cleared with the report
     g.close()
+
+
+def test_pin_host_from_the_library():
+    """tg_pin_host page-locks the bound arrays (the overlapped form then
+    runs) and is harmless when repeated; results stay bit-exact"""
+    cfg = small_cfg(2, 3, fixed=1)
+    ions, lecs = beams(cfg)
+    f = random_fields(cfg, np.random.default_rng(24), scale=0.02)
+    o, g0 = pair(cfg, ions, lecs, f)
+    g0.close()
+    g = host_sim(cfg, ions, lecs, f, False)
+    g.pin_host()
+    g.pin_host()
+    g.step_host(3)
+    o.step(3)
+    assert_fields_equal(o, g, ALL)
+    assert_particles_equal(g.ions, o.ions)
+    assert_particles_equal(g.lecs, o.lecs)
+    g.close()

@@ -84,6 +84,7 @@ struct tg_ctx {
     cudaEvent_t ev_link[5] = {};
     void *stage2 = nullptr;
     long long host_n[2] = {0, 0};
+    std::vector<void *> pinned;  // host ranges page-locked by tg_pin_host
     char err[512] = {0};
     std::vector<void *> allocs;
 };
@@ -355,6 +356,7 @@ extern "C" void tg_finalize(tg_ctx *ctx) {
     if (ctx->cub_tmp) cudaFree(ctx->cub_tmp);
     for (auto &e : ctx->ev_link)
         if (e) cudaEventDestroy(e);
+    for (void *h : ctx->pinned) cudaHostUnregister(h);
     if (ctx->st_up) cudaStreamDestroy(ctx->st_up);
     if (ctx->st_down) cudaStreamDestroy(ctx->st_down);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -1274,6 +1276,34 @@ static int host_lap(tg_ctx *ctx) {
     }
     *ctx->hions = (int32_t)n[0];
     *ctx->hlecs = (int32_t)n[1];
+    return TG_OK;
+}
+
+extern "C" int tg_pin_host(tg_ctx *ctx) {
+    if (!ctx) return TG_ERR_ARG;
+    if (!ctx->hp) return fail(ctx, TG_ERR_STATE, "tg_pin_host: particles not bound");
+    void *h[10];
+    size_t len[10];
+    int n = 0;
+    for (int a = 0; a < 9; a++)
+        if (ctx->hf[a]) {
+            h[n] = ctx->hf[a];
+            len[n++] = (size_t)ctx->g.lot * 4;
+        }
+    h[n] = ctx->hp;
+    len[n++] = (size_t)ctx->cfg.maxhlf * AOS * 2;
+    for (int i = 0; i < n; i++) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, h[i]) == cudaSuccess && at.type == cudaMemoryTypeHost) continue;
+        (void)cudaGetLastError();
+        cudaError_t e = cudaHostRegister(h[i], len[i], cudaHostRegisterDefault);
+        if (e == cudaErrorHostMemoryAlreadyRegistered) {
+            (void)cudaGetLastError();
+            continue;
+        }
+        if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_pin_host: cudaHostRegister: %s", cudaGetErrorString(e));
+        ctx->pinned.push_back(h[i]);
+    }
     return TG_OK;
 }
 

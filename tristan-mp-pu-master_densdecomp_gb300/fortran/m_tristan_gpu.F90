@@ -138,6 +138,15 @@ module m_tristan_gpu_3d
        type(c_ptr), value :: ctx
        integer(c_int32_t), value :: nsteps
      end function
+     integer(c_int) function tg_step_host(ctx, nsteps) bind(C, name="tg_step_host")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: nsteps
+     end function
+     integer(c_int) function tg_pin_host(ctx) bind(C, name="tg_pin_host")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
      ! collisionless-shock hooks (user_pu/user_shock_pu.F90)
      integer(c_int) function tg_shock_init(ctx, k) bind(C, name="tg_shock_init")
        import :: c_int, c_ptr, tg_shock
@@ -200,10 +209,10 @@ module m_tristan_gpu_3d
   type(c_ptr), save :: ctx = c_null_ptr
   integer(c_int), parameter :: SYNC_E = 1, SYNC_B = 2, SYNC_CUR = 4, SYNC_PARTICLES = 8, SYNC_ALL = 15
 
-  public :: tg_start, tg_stop, tg_download, tg_upload, &
+  public :: tg_start, tg_stop, tg_download, tg_upload, tg_pin, &
             gpu_bc_b1, gpu_bc_e1, gpu_advance_Bhalfstep, gpu_advance_Efield, gpu_move_particles, &
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
-            gpu_add_current, gpu_reorder_particles, gpu_step, &
+            gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
             gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
             gpu_write_restart, gpu_read_restart, gpu_meanq
 
@@ -265,6 +274,11 @@ contains
     call tg_finalize(ctx)
     ctx = c_null_ptr
   end subroutine tg_stop
+
+  ! page-lock ex..curz and p (asynchronous DMA for gpu_step_host and the syncs)
+  subroutine tg_pin()
+    call check(tg_pin_host(ctx), "tg_pin_host")
+  end subroutine tg_pin
 
   ! before Diagnostics / output / restart / host-side user hooks
   subroutine tg_download()
@@ -350,6 +364,14 @@ contains
   subroutine gpu_step(nsteps)
     integer, intent(in) :: nsteps
     call check(tg_step(ctx, int(nsteps, c_int32_t)), "tg_step")
+  end subroutine
+
+  ! one main-loop pass with the module's own arrays as the state: ex..bz and
+  ! the particle records go to the device, the lap runs, ex..curz, the
+  ! records and ions / lecs come back (tg_step_host)
+  subroutine gpu_step_host(nsteps)
+    integer, intent(in) :: nsteps
+    call check(tg_step_host(ctx, int(nsteps, c_int32_t)), "tg_step_host")
   end subroutine
 
 #ifdef twoD

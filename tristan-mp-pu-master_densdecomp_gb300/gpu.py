@@ -114,7 +114,7 @@ ENTRY_POINTS = (
     "tg_init", "tg_finalize", "tg_last_error", "tg_bind_fields", "tg_bind_particles",
     "tg_sync_from_host", "tg_sync_to_host", "tg_bc_b1", "tg_bc_e1", "tg_advance_b_half",
     "tg_advance_e", "tg_move", "tg_reset_currents", "tg_deposit", "tg_fold_currents",
-    "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_step_host", "tg_diag_fp64", "tg_synchronize",
+    "tg_filter", "tg_add_current", "tg_reorder", "tg_step", "tg_step_host", "tg_pin_host", "tg_diag_fp64", "tg_synchronize",
     "tg_get_counts", "tg_device_fields", "tg_stream", "tg_kernels_per_step", "tg_diag_history",
     "tg_enable_timing", "tg_phase_times", "tg_step_timed", "tg_filter_noalloc", "tg_autotune",
     "tg_ens_init", "tg_ens_finalize", "tg_ens_last_error", "tg_ens_bind_fields", "tg_ens_bind_particles",
@@ -161,6 +161,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_step.restype = ctypes.c_int
     lib.tg_step_host.argtypes = [P, ctypes.c_int32]
     lib.tg_step_host.restype = ctypes.c_int
+    lib.tg_pin_host.argtypes = [P]
+    lib.tg_pin_host.restype = ctypes.c_int
     lib.tg_diag_fp64.argtypes = [P, ctypes.POINTER(tg_diag)]
     lib.tg_diag_fp64.restype = ctypes.c_int
     lib.tg_get_counts.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
@@ -451,6 +453,10 @@ class GpuSim:
         """n main-loop passes with the host arrays as the state (tg_step_host):
         E, B and the records up, the lap, everything back, every lap"""
         self._check(self.lib.tg_step_host(self.h, int(n)))
+
+    def pin_host(self):
+        """page-lock the bound host arrays from the library (tg_pin_host)"""
+        self._check(self.lib.tg_pin_host(self.h))
 
     def step_timed(self, n: int) -> float:
         """n laps bracketed by CUDA events on the library's stream; ms"""
