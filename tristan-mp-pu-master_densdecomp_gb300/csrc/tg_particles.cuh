@@ -78,15 +78,18 @@ __device__ __forceinline__ void store_pos(const Geom &g, const Species &s, long 
 }
 
 // warp-aggregated atomicAdd of 1 to counter[key]; returns this lane's slot.
-// Lanes are grouped by key alone: every active lane must pass the same
-// counter array.
+// Lanes are grouped by the counter's address: with independent thread
+// scheduling the lanes that arrive together may come from different loop
+// iterations (another species' counter array), so the key alone is not
+// enough.
 __device__ __forceinline__ int agg_inc(int *counter, int key) {
+    int *const addr = counter + key;
     const unsigned active = __activemask();
-    const unsigned peers = __match_any_sync(active, key);
+    const unsigned peers = __match_any_sync(active, (unsigned long long)(uintptr_t)addr);
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
     int base = 0;
-    if (lane == leader) base = atomicAdd(counter + key, __popc(peers));
+    if (lane == leader) base = atomicAdd(addr, __popc(peers));
     base = __shfl_sync(peers, base, leader);
     return base + __popc(peers & ((1u << lane) - 1u));
 }
