@@ -360,6 +360,23 @@ int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz,
 int tg_spectrum_dims(tg_ctx *ctx, int32_t gambins, int32_t *nxbins, int32_t *nybins);
 int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *xgamma, float *xslice,
                 float *yslice, float *gamma_range);
+/* Energy spectra per x slice for the spectrum output (save_spectrum,
+   code/output.F90:380-785, the writer the reference's output calls):
+   nbins = max((mx0 - 5) / 100, 1) slices of x in [3, mx0 - 2] (all y);
+   gambins logarithmic bins of gamma - 1 over the gamma range of every
+   particle; per species the lab-frame spectrum (spec_ions, spec_lecs:
+   "specp", "spece") and the spectrum in each slice's mean-flow frame
+   (spec_*_rest: "specprest", "specerest"), weights splitratio^(1 -
+   splitlev) ch with the legacy splitratio = 10, every bin divided by its
+   gamma - 1 (xgamma) as the reference does. tg_spectrum_x_bins gives
+   nbins; spec_* hold nbins*gambins floats (slice fastest), xgamma gambins,
+   xslice nbins, gamma_range (may be NULL) [gammin, gammax]. The
+   reference's electron loops start one record early (p(maxhlf), the last
+   ion slot, zero unless the ion array is full); that record is not
+   counted. Synchronises. */
+int tg_spectrum_x_bins(tg_ctx *ctx, int32_t *nbins);
+int tg_spectrum_x(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *spec_ions_rest,
+                  float *spec_lecs_rest, float *xgamma, float *xslice, float *gamma_range);
 
 /* ---------------------------------------------------------------------
    Batched ensemble: many independent periodic 2D boxes of uneven size

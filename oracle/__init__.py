@@ -159,6 +159,11 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_spectrum_2d.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5 + \
                 [ctypes.POINTER(ctypes.c_float)] * 2
             lib.to_spectrum_2d.restype = None
+            lib.to_spectrum_x_bins.argtypes = [P]
+            lib.to_spectrum_x_bins.restype = ctypes.c_int
+            lib.to_spectrum_x.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 6 + \
+                [ctypes.POINTER(ctypes.c_float)] * 2
+            lib.to_spectrum_x.restype = None
             K = ctypes.POINTER(to_shock)
             lib.to_random.argtypes = [ctypes.POINTER(ctypes.c_double)]
             lib.to_random.restype = ctypes.c_float
@@ -318,6 +323,18 @@ class OracleSim:
         self.lib.to_spectrum_2d(self.ptr, gambins, si.ctypes.data, se.ctypes.data, xg.ctypes.data, xs.ctypes.data,
                                 ys.ctypes.data, ctypes.byref(gmin), ctypes.byref(gmax))
         return dict(ions=si, lecs=se, xgamma=xg, xslice=xs, yslice=ys, gammin=gmin.value, gammax=gmax.value)
+
+    def spectrum_x(self, gambins: int = 200) -> dict:
+        """save_spectrum: per x slice, lab-frame and flow-frame spectra"""
+        nb = self.lib.to_spectrum_x_bins(self.ptr)
+        out = {k: np.zeros((gambins, nb), np.float32) for k in ("ions", "lecs", "ions_rest", "lecs_rest")}
+        xg = np.zeros(gambins, np.float32)
+        xs = np.zeros(nb, np.float32)
+        gmin, gmax = ctypes.c_float(), ctypes.c_float()
+        self.lib.to_spectrum_x(self.ptr, gambins, out["ions"].ctypes.data, out["lecs"].ctypes.data,
+                               out["ions_rest"].ctypes.data, out["lecs_rest"].ctypes.data, xg.ctypes.data,
+                               xs.ctypes.data, ctypes.byref(gmin), ctypes.byref(gmax))
+        return dict(out, xgamma=xg, xslice=xs, gammin=gmin.value, gammax=gmax.value)
 
     def charge_density(self) -> np.ndarray:
         rho = np.zeros(self.lot, np.float64)

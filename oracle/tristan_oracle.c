@@ -1625,6 +1625,99 @@ int to_spectrum_dims(const to_state *s, int gambins, int *nx, int *ny)
 
 /* spec_i / spec_e: nxbins*nybins*gambins (x fastest); xgamma: gambins;
    xslice / yslice: nxbins / nybins; returns gammin and gammax */
+/* save_spectrum (code/output.F90:380-785): x slices of about 100 cells over
+   [3, mx0 - 2], lab-frame and mean-flow-frame spectra per species, weights
+   splitratio^(1 - splitlev) ch (splitratio = 10, code/particles.F90:336),
+   each bin divided by its gamma - 1. The electron loops start at p(maxhlf)
+   as the reference's do (one record before the first electron). */
+int to_spectrum_x_bins(const to_state *s)
+{
+    const int nb = (s->mx - 2 - 3) / 100;
+    return nb > 1 ? nb : 1;
+}
+
+void to_spectrum_x(const to_state *s, int gambins, float *spec_i, float *spec_e, float *rest_i, float *rest_e,
+                   float *xgamma, float *xslice, float *gmin_out, float *gmax_out)
+{
+    const int mxmin = 3, mxmax = s->mx - 2;
+    const int nbins = to_spectrum_x_bins(s);
+    const float dxslice = 1.0f * (float)(mxmax - mxmin) / (float)nbins;
+    for (int i = 1; i <= nbins; i++) xslice[i - 1] = dxslice * (float)(i - 1) + 0.5f * dxslice + (float)mxmin;
+    float gammin = 1.0f, gammax = 1.0f;
+    for (int sp = 0; sp < 2; sp++) {
+        const int64_t base = sp == 0 ? 0 : s->maxhlf, cnt = sp == 0 ? s->ions : s->lecs;
+        for (int64_t n = 0; n < cnt; n++) {
+            const to_particle *p = &s->p[base + n];
+            const float gam = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+            if (gam > gammax) gammax = gam;
+            if (gam < gammin) gammin = gam;
+        }
+    }
+    gammin = fmaxf(gammin, 1.0f + 1e-6f);
+    const float lg0 = to_log10f(gammin - 1.0f);
+    const float dgam = (to_log10f(gammax - 1.0f) - lg0) / (float)gambins;
+    for (int i = 1; i <= gambins; i++) xgamma[i - 1] = powf(10.0f, (float)(i - 1) * dgam + lg0);
+    float *um = calloc((size_t)nbins * 4, sizeof(float));
+    float *vm = um + nbins, *wm = vm + nbins, *nd = wm + nbins;
+    for (int sp = 0; sp < 2; sp++) {
+        float *lab = sp == 0 ? spec_i : spec_e, *rest = sp == 0 ? rest_i : rest_e;
+        memset(lab, 0, sizeof(float) * (size_t)nbins * gambins);
+        memset(rest, 0, sizeof(float) * (size_t)nbins * gambins);
+        memset(um, 0, sizeof(float) * (size_t)nbins * 4);
+        /* ions: p(1..ions); electrons: p(maxhlf..maxhlf+lecs) */
+        const int64_t first = sp == 0 ? 0 : s->maxhlf - 1, last = sp == 0 ? s->ions : s->maxhlf + s->lecs;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int64_t n = first; n < last; n++) {
+                const to_particle *p = &s->p[n];
+                const float fxb = (p->x + (float)s->mxcum - (float)mxmin) / dxslice + 1.0f;
+                if (!(fxb >= 1.0f)) continue;
+                const int xbin = (int)fxb;
+                if (xbin > nbins) continue;
+                const int64_t sl = xbin - 1;
+                const float w = powf(10.0f, 1.0f - (float)p->splitlev);
+                const float gam = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+                if (pass == 0) {
+                    nd[sl] = nd[sl] + w * p->ch;
+                    um[sl] = um[sl] + (p->u / gam) * w * p->ch;
+                    vm[sl] = vm[sl] + (p->v / gam) * w * p->ch;
+                    wm[sl] = wm[sl] + (p->w / gam) * w * p->ch;
+                    continue;
+                }
+                const float fl = (to_log10f(gam - 1.0f) - lg0) / dgam + 1.0f;
+                if (fl >= 1.0f && fl < (float)gambins + 1.0f)
+                    lab[sl + nbins * ((int)fl - 1)] = lab[sl + nbins * ((int)fl - 1)] + w * p->ch;
+                const float vx = um[sl], vy = vm[sl], vz = wm[sl];
+                const float vr = sqrtf(vx * vx + vy * vy + vz * vz);
+                const float gvr = 1.0f / sqrtf(1.0f - vr * vr);
+                const float vr2 = vr * vr;
+                const float uprime = -vx * gvr * gam + (1.0f + (gvr - 1.0f) * (vx * vx) / vr2) * p->u +
+                                     (gvr - 1.0f) * vx * vy / vr2 * p->v + (gvr - 1.0f) * vx * vz / vr2 * p->w;
+                const float vprime = -vy * gvr * gam + (gvr - 1.0f) * vx * vy / vr2 * p->u +
+                                     (1.0f + (gvr - 1.0f) * (vy * vy) / vr2) * p->v + (gvr - 1.0f) * vy * vz / vr2 * p->w;
+                const float wprime = -vz * gvr * gam + (gvr - 1.0f) * vx * vz / vr2 * p->u +
+                                     (gvr - 1.0f) * vy * vz / vr2 * p->v + (1.0f + (gvr - 1.0f) * (vz * vz) / vr2) * p->w;
+                const float gp = sqrtf(1.0f + (uprime * uprime + vprime * vprime + wprime * wprime));
+                const float fg = (to_log10f(gp - 1.0f) - lg0) / dgam + 1.0f;
+                if (!(fg >= 1.0f && fg < (float)gambins + 1.0f)) continue;
+                rest[sl + nbins * ((int)fg - 1)] = rest[sl + nbins * ((int)fg - 1)] + w * p->ch;
+            }
+            if (pass == 0)
+                for (int64_t l = 0; l < nbins; l++) {
+                    um[l] = um[l] / nd[l];
+                    vm[l] = vm[l] / nd[l];
+                    wm[l] = wm[l] / nd[l];
+                }
+        }
+        for (int64_t t = 0; t < (int64_t)nbins * gambins; t++) {
+            lab[t] = lab[t] / xgamma[t / nbins];
+            rest[t] = rest[t] / xgamma[t / nbins];
+        }
+    }
+    free(um);
+    *gmin_out = gammin;
+    *gmax_out = gammax;
+}
+
 void to_spectrum_2d(const to_state *s, int gambins, float *spec_i, float *spec_e, float *xgamma, float *xslice,
                     float *yslice, float *gmin_out, float *gmax_out)
 {

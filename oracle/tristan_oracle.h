@@ -210,6 +210,11 @@ void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, floa
    code/output.F90:794-1249); dims from to_spectrum_dims */
 float to_log10f(float x);
 int to_spectrum_dims(const to_state *s, int gambins, int *nx, int *ny);
+/* save_spectrum (code/output.F90:380-785): x slices, lab-frame and
+   flow-frame spectra, divided by gamma - 1 */
+int to_spectrum_x_bins(const to_state *s);
+void to_spectrum_x(const to_state *s, int gambins, float *spec_i, float *spec_e, float *rest_i, float *rest_e,
+                   float *xgamma, float *xslice, float *gmin_out, float *gmax_out);
 void to_spectrum_2d(const to_state *s, int gambins, float *spec_i, float *spec_e, float *xgamma, float *xslice,
                     float *yslice, float *gmin_out, float *gmax_out);
 /* sin and cos of a float argument, evaluated in double and rounded once */

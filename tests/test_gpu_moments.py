@@ -85,3 +85,44 @@ def test_flow_frame_spectra_match_oracle():
         assert abs(a.sum() - tot) <= 2
         assert np.abs(a - b).sum() <= max(4.0, 2e-3 * tot), sp
     g.close()
+
+
+def test_x_slice_spectra_match_oracle():
+    """save_spectrum (the writer the reference's output calls) on the device:
+    x slices of about 100 cells, lab-frame and flow-frame spectra with the
+    splitratio^(1 - splitlev) weights, divided by gamma - 1. Axes and the
+    gamma range equal the oracle's; lab-frame bins are the same per
+    particle, so the sums agree to FP32 summation order; flow-frame bins
+    move by a few per mille of the weight at most, as for the 2D writer"""
+    from tristan_gb300.gpu import GpuSim
+    cfg = small_cfg(2, 3, fixed=1, nx=320, ny=16, ppc0=8.0)
+    ions, lecs = beams(cfg)
+    ions["splitlev"][::7] = 2   # weight 0.1
+    lecs["splitlev"][::5] = 3   # weight 0.01
+    f = random_fields(cfg, np.random.default_rng(5), scale=0.02)
+    o = oracle.OracleSim(cfg)
+    for k, v in f.items():
+        o.fields[k][:] = v
+    o.set_particles(ions, lecs)
+    g = GpuSim(cfg)
+    g.set_fields(**f)
+    g.sync_from_host()
+    g.set_particles(ions, lecs)
+    g.step(5)
+    o.step(5)
+    gs = g.spectrum_x()
+    os_ = o.spectrum_x()
+    assert gs["xslice"].size == 3
+    for k in ("xgamma", "xslice"):
+        np.testing.assert_array_equal(gs[k], os_[k], err_msg=k)
+    assert gs["gammin"] == os_["gammin"] and gs["gammax"] == os_["gammax"]
+    xg = gs["xgamma"].astype(np.float64)[:, None]
+    for sp in ("ions", "lecs"):
+        lab_g, lab_o = gs[sp] * xg, os_[sp] * xg
+        tot = lab_o.sum()
+        assert tot > 1000
+        np.testing.assert_allclose(lab_g, lab_o, rtol=1e-5, atol=1e-6 * tot, err_msg=sp)
+        rest_g, rest_o = gs[sp + "_rest"] * xg, os_[sp + "_rest"] * xg
+        assert abs(rest_g.sum() - rest_o.sum()) <= 1e-5 * tot + 2
+        assert np.abs(rest_g - rest_o).sum() <= max(4.0, 2e-3 * tot), sp
+    g.close()

@@ -112,3 +112,30 @@ def test_yee_vacuum_dispersion():
     w_meas = 2 * math.pi / period
     w_theory = 2 * math.asin(cfg.corr * cfg.c * math.sin(kk / 2))
     assert abs(w_meas - w_theory) / w_theory < 2e-3
+
+
+def test_x_slice_spectrum_weights_and_axes():
+    """save_spectrum's restatement: the slices tile [3, mx0 - 2], the
+    lab-frame spectrum times gamma - 1 holds the splitratio^(1 - splitlev)
+    weights of every particle inside them but the one at gammax (its bin is
+    gambins + 1), and the flow-frame spectrum holds the same total up to the
+    particles that leave the gamma range in that frame"""
+    from test_gpu_parity import beams, small_cfg
+    cfg = small_cfg(2, 2, fixed=1, nx=320, ny=16, ppc0=8.0)
+    ions, lecs = beams(cfg)
+    ions["splitlev"][::7] = 2
+    lecs["splitlev"][::5] = 3
+    o = oracle.OracleSim(cfg)
+    o.set_particles(ions, lecs)
+    s = o.spectrum_x(gambins=200)
+    nb = s["xslice"].size
+    assert nb == (cfg.mx - 5) // 100
+    dx = (cfg.mx - 5) / nb
+    np.testing.assert_allclose(s["xslice"], 3 + dx * (np.arange(nb) + 0.5), rtol=1e-6)
+    xg = s["xgamma"].astype(np.float64)[:, None]
+    for sp, p in (("ions", ions), ("lecs", lecs)):
+        w = (10.0 ** (1.0 - p["splitlev"].astype(np.float64))) * p["ch"]
+        inside = (p["x"] >= 3) & (p["x"] < 3 + nb * dx)
+        lab = (s[sp] * xg).sum()
+        assert abs(lab - w[inside].sum()) <= 1.0 + 1e-5 * lab, sp
+        assert abs((s[sp + "_rest"] * xg).sum() - lab) <= 0.01 * lab, sp

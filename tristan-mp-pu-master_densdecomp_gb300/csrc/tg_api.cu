@@ -1653,21 +1653,26 @@ extern "C" int tg_spectrum_dims(tg_ctx *ctx, int32_t gambins, int32_t *nxbins, i
     return TG_OK;
 }
 
-extern "C" int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *xgamma,
-                           float *xslice, float *yslice, float *gamma_range) {
-    if (!ctx || !spec_ions || !spec_lecs || !xgamma || !xslice || !yslice || gambins < 1) return TG_ERR_ARG;
-    const SpecGrid sg = spec_grid(ctx->g.mx, ctx->g.my, ctx->g.ng, gambins);
+// One spectrum pass over the slice grid sg: the gamma range over every
+// particle, then per species the slice-mean velocities and the histograms
+// (flow frame into rest[s], lab frame into lab[s] when given); with
+// per_xgamma every bin is divided by its gamma - 1 (xgamma), as
+// save_spectrum does. yslice may be NULL.
+static int spectrum_run(tg_ctx *ctx, const SpecGrid &sg, float *const rest[2], float *const lab[2], float *xgamma,
+                        float *xslice, float *yslice, float *gamma_range, bool per_xgamma, const char *who) {
+    const int gambins = sg.gambins;
     const long long nsl = (long long)sg.nxb * sg.nyb;
     long long n[2];
     int r = exact_counts(ctx, n);
     if (r) return r;
-    // scratch: 4 FP64 sums and 3 means per slice, the gamma range, the histogram
+    // scratch: 4 FP64 sums and 3 means per slice, the gamma range, the histograms
     double *acc = nullptr;
     float *mean = nullptr, *spec = nullptr;
     unsigned *range = nullptr;
+    const size_t hbytes = (size_t)nsl * gambins * 4;
     cudaError_t e = cudaMalloc(&acc, (size_t)nsl * 4 * 8);
     if (e == cudaSuccess) e = cudaMalloc(&mean, (size_t)nsl * 3 * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&spec, (size_t)nsl * gambins * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&spec, 2 * hbytes);
     if (e == cudaSuccess) e = cudaMalloc(&range, 8);
     const unsigned one = 0x3f800000u;  // 1.0f
     const unsigned init[2] = {one, one};
@@ -1685,24 +1690,55 @@ extern "C" int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float
     const float dgam = (log10_single(gmax - 1.0f) - lg0) / (float)gambins;
     for (int i = 1; i <= gambins; i++) xgamma[i - 1] = powf(10.0f, (float)(i - 1) * dgam + lg0);
     for (int i = 1; i <= sg.nxb; i++) xslice[i - 1] = sg.dxslice * (float)(i - 1) + 0.5f * sg.dxslice + (float)sg.mxmin;
-    for (int i = 1; i <= sg.nyb; i++) yslice[i - 1] = sg.dyslice * (float)(i - 1) + 0.5f * sg.dyslice + (float)sg.mymin;
+    if (yslice)
+        for (int i = 1; i <= sg.nyb; i++)
+            yslice[i - 1] = sg.dyslice * (float)(i - 1) + 0.5f * sg.dyslice + (float)sg.mymin;
     if (gamma_range) {
         gamma_range[0] = gammin;
         gamma_range[1] = gmax;
     }
     for (int s = 0; s < 2 && e == cudaSuccess; s++) {
-        float *out = s == 0 ? spec_ions : spec_lecs;
-        e = cudaMemsetAsync(spec, 0, (size_t)nsl * gambins * 4, ctx->st);
+        float *spec_lab = lab[s] ? spec + (size_t)nsl * gambins : nullptr;
+        e = cudaMemsetAsync(spec, 0, 2 * hbytes, ctx->st);
         if (e == cudaSuccess)
             e = launch_spec_species(ctx->g, ctx->P, sg, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,
-                                    n[s], acc, mean, lg0, dgam, spec, ctx->st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(out, spec, (size_t)nsl * gambins * 4, cudaMemcpyDeviceToHost, ctx->st);
+                                    n[s], acc, mean, lg0, dgam, spec, spec_lab, ctx->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(rest[s], spec, hbytes, cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess && lab[s]) e = cudaMemcpyAsync(lab[s], spec_lab, hbytes, cudaMemcpyDeviceToHost, ctx->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e == cudaSuccess && per_xgamma)
+            for (long long t = 0; t < nsl * gambins; t++) {
+                rest[s][t] = rest[s][t] / xgamma[t / nsl];
+                if (lab[s]) lab[s][t] = lab[s][t] / xgamma[t / nsl];
+            }
     }
     cudaFree(acc);
     cudaFree(mean);
     cudaFree(spec);
     cudaFree(range);
-    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_spectrum: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "%s: %s", who, cudaGetErrorString(e));
     return check_status(ctx);
+}
+
+extern "C" int tg_spectrum(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *xgamma,
+                           float *xslice, float *yslice, float *gamma_range) {
+    if (!ctx || !spec_ions || !spec_lecs || !xgamma || !xslice || !yslice || gambins < 1) return TG_ERR_ARG;
+    const SpecGrid sg = spec_grid(ctx->g.mx, ctx->g.my, ctx->g.ng, gambins);
+    float *rest[2] = {spec_ions, spec_lecs}, *lab[2] = {nullptr, nullptr};
+    return spectrum_run(ctx, sg, rest, lab, xgamma, xslice, yslice, gamma_range, false, "tg_spectrum");
+}
+
+extern "C" int tg_spectrum_x_bins(tg_ctx *ctx, int32_t *nbins) {
+    if (!ctx || !nbins) return TG_ERR_ARG;
+    *nbins = spec_grid_x(ctx->g.mx, 1).nxb;
+    return TG_OK;
+}
+
+extern "C" int tg_spectrum_x(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_lecs, float *spec_ions_rest,
+                             float *spec_lecs_rest, float *xgamma, float *xslice, float *gamma_range) {
+    if (!ctx || !spec_ions || !spec_lecs || !spec_ions_rest || !spec_lecs_rest || !xgamma || !xslice || gambins < 1)
+        return TG_ERR_ARG;
+    const SpecGrid sg = spec_grid_x(ctx->g.mx, gambins);
+    float *rest[2] = {spec_ions_rest, spec_lecs_rest}, *lab[2] = {spec_ions, spec_lecs};
+    return spectrum_run(ctx, sg, rest, lab, xgamma, xslice, nullptr, gamma_range, true, "tg_spectrum_x");
 }

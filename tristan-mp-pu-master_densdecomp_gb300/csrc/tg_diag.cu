@@ -333,6 +333,13 @@ __device__ __forceinline__ bool spec_slice(const SpecGrid &sg, float x, float y,
     return true;
 }
 
+// the spectrum weight of particle n: ch, or splitratio^(1 - splitlev) ch
+__device__ __forceinline__ float spec_w(const SpecGrid &sg, const Species &sp, long long n) {
+    if (!sg.split) return 1.0f;
+    const int s = sp.splitlev[n];
+    return (s >= 0 && s < 32) ? sg.wsplit[s] : powf(10.0f, 1.0f - (float)s);
+}
+
 // gamma range over every particle (starting from 1, as the reference)
 __global__ void __launch_bounds__(256) k_spec_range(Species si, Species se, const long long *count,
                                                     unsigned *gmin, unsigned *gmax) {
@@ -364,17 +371,18 @@ __global__ void __launch_bounds__(256) k_spec_means(Geom g, Params P, SpecGrid s
     const long long nsl = (long long)sg.nxb * sg.nyb;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < *count;
          n += (long long)gridDim.x * blockDim.x) {
-        if (sp.cell[n] < 0 || sp.ind[n] <= 0) continue;
+        if (sp.cell[n] < 0 || (sg.ind_filter && sp.ind[n] <= 0)) continue;
         float x, y, z;
         load_pos<DIM>(g, sp, n, x, y, z);
         int sl;
         if (!spec_slice(sg, x, y, P.mxcum, P.mycum, sl)) continue;
         const float u = sp.u[n], v = sp.v[n], w = sp.w[n], ch = sp.ch[n];
+        const float ws = spec_w(sg, sp, n);  // 1 unless split weights: products exact then
         const float gam = sqrtf(1.0f + (u * u + v * v + w * w));
-        atomicAdd(acc + sl, (double)ch);
-        atomicAdd(acc + nsl + sl, (double)((u / gam) * ch));
-        atomicAdd(acc + 2 * nsl + sl, (double)((v / gam) * ch));
-        atomicAdd(acc + 3 * nsl + sl, (double)((w / gam) * ch));
+        atomicAdd(acc + sl, (double)(ws * ch));
+        atomicAdd(acc + nsl + sl, (double)((u / gam) * ws * ch));
+        atomicAdd(acc + 2 * nsl + sl, (double)((v / gam) * ws * ch));
+        atomicAdd(acc + 3 * nsl + sl, (double)((w / gam) * ws * ch));
     }
 }
 
@@ -388,19 +396,27 @@ __global__ void k_spec_divide(long long nsl, double *acc, float *mean) {
     }
 }
 
+// per particle: the flow-frame gamma bin (and with spec_lab, the lab-frame
+// one) gets the particle's weight
 template <int DIM>
 __global__ void __launch_bounds__(256) k_spec_bins(Geom g, Params P, SpecGrid sg, Species sp, const long long *count,
-                                                   const float *mean, float lg0, float dgam, float *spec) {
+                                                   const float *mean, float lg0, float dgam, float *spec,
+                                                   float *spec_lab) {
     const long long nsl = (long long)sg.nxb * sg.nyb;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < *count;
          n += (long long)gridDim.x * blockDim.x) {
-        if (sp.cell[n] < 0 || sp.ind[n] <= 0) continue;
+        if (sp.cell[n] < 0 || (sg.ind_filter && sp.ind[n] <= 0)) continue;
         float x, y, z;
         load_pos<DIM>(g, sp, n, x, y, z);
         int sl;
         if (!spec_slice(sg, x, y, P.mxcum, P.mycum, sl)) continue;
         const float u = sp.u[n], v = sp.v[n], w = sp.w[n], ch = sp.ch[n];
+        const float wt = spec_w(sg, sp, n) * ch;
         const float gam = sqrtf(1.0f + (u * u + v * v + w * w));
+        if (spec_lab) {
+            const float fl = (log10_single(gam - 1.0f) - lg0) / dgam + 1.0f;
+            if (fl >= 1.0f && fl < (float)sg.gambins + 1.0f) atomicAdd(spec_lab + sl + nsl * ((int)fl - 1), wt);
+        }
         const float vx = mean[sl], vy = mean[nsl + sl], vz = mean[2 * nsl + sl];
         const float vr = sqrtf(vx * vx + vy * vy + vz * vz);
         const float gvr = 1.0f / sqrtf(1.0f - vr * vr);
@@ -415,7 +431,7 @@ __global__ void __launch_bounds__(256) k_spec_bins(Geom g, Params P, SpecGrid sg
         const float fg = (log10_single(gp - 1.0f) - lg0) / dgam + 1.0f;
         if (!(fg >= 1.0f && fg < (float)sg.gambins + 1.0f)) continue;
         const int gbin = (int)fg;
-        atomicAdd(spec + sl + nsl * (gbin - 1), ch);
+        atomicAdd(spec + sl + nsl * (gbin - 1), wt);
     }
 }
 
@@ -429,16 +445,16 @@ cudaError_t launch_spec_range(const Species *sp, const long long *count, long lo
 
 cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &sg, const Species &sp,
                                 const long long *count, long long hint, double *acc, float *mean, float lg0,
-                                float dgam, float *spec, cudaStream_t st) {
+                                float dgam, float *spec, float *spec_lab, cudaStream_t st) {
     const long long nsl = (long long)sg.nxb * sg.nyb;
     if (g.dims == 3) {
         k_spec_means<3><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, acc);
         k_spec_divide<<<dgrid(nsl), 256, 0, st>>>(nsl, acc, mean);
-        k_spec_bins<3><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec);
+        k_spec_bins<3><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec, spec_lab);
     } else {
         k_spec_means<2><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, acc);
         k_spec_divide<<<dgrid(nsl), 256, 0, st>>>(nsl, acc, mean);
-        k_spec_bins<2><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec);
+        k_spec_bins<2><<<dgrid(hint), 256, 0, st>>>(g, P, sg, sp, count, mean, lg0, dgam, spec, spec_lab);
     }
     return cudaGetLastError();
 }

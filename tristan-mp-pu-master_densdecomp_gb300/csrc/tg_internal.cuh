@@ -473,7 +473,7 @@ cudaError_t launch_spec_range(const Species *sp, const long long *count, long lo
                               cudaStream_t st);
 cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &sg, const Species &sp,
                                 const long long *count, long long hint, double *acc, float *mean, float lg0,
-                                float dgam, float *spec, cudaStream_t st);
+                                float dgam, float *spec, float *spec_lab, cudaStream_t st);
 // grid moments (meanq_fld_cur) into f3[0] (moment) and f3[1] (weight);
 // num / den are zeroed FP64 scratch of g.lot cells, left zeroed
 cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,

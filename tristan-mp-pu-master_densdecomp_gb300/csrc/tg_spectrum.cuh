@@ -24,11 +24,15 @@ __host__ __device__ inline float log10_single(float x) {
     return (float)(ln / 2.30258509299404568402);
 }
 
-// slice layout of save_spectrum_2d (code/output.F90:828-852)
+// slice layout and particle weights of a spectrum writer
 struct SpecGrid {
     int mxmin, mymin, nxb, nyb, gambins;
     float dxslice, dyslice;
+    int ind_filter;    // only particles with ind > 0 count (save_spectrum_2d)
+    int split;         // weight splitratio^(1 - splitlev) * ch (save_spectrum)
+    float wsplit[32];  // splitratio^(1 - s) for splitlev s in [0, 32)
 };
+// save_spectrum_2d (code/output.F90:828-852): slices of 30 cells
 
 inline SpecGrid spec_grid(int mx, int my, int ng, int gambins) {
     SpecGrid s;
@@ -42,6 +46,28 @@ inline SpecGrid spec_grid(int mx, int my, int ng, int gambins) {
     s.gambins = gambins;
     s.dxslice = 1.0f * (float)(mxmax - mxmin) / (float)s.nxb;
     s.dyslice = 1.0f * (float)(mymax - mymin) / (float)s.nyb;
+    s.ind_filter = 1;
+    s.split = 0;
+    for (int k = 0; k < 32; k++) s.wsplit[k] = 1.0f;
+    return s;
+}
+// save_spectrum (code/output.F90:424-437): x slices of about 100 cells over
+// [3, mx0 - 2], one slice in y; weights splitratio^(1 - splitlev) ch with
+// the legacy splitratio = 10 (code/particles.F90:336), powers from the
+// host's powf as the reference's real**real
+inline SpecGrid spec_grid_x(int mx, int gambins) {
+    SpecGrid s;
+    const int mxmin = 3, mxmax = mx - 2;
+    s.mxmin = mxmin;
+    s.mymin = 0;
+    s.nxb = (mxmax - mxmin) / 100 > 1 ? (mxmax - mxmin) / 100 : 1;
+    s.nyb = 1;
+    s.gambins = gambins;
+    s.dxslice = 1.0f * (float)(mxmax - mxmin) / (float)s.nxb;
+    s.dyslice = INFINITY;  // every y in the one slice
+    s.ind_filter = 0;
+    s.split = 1;
+    for (int k = 0; k < 32; k++) s.wsplit[k] = powf(10.0f, 1.0f - (float)k);
     return s;
 }
 

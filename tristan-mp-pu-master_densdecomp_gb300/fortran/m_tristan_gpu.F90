@@ -194,6 +194,18 @@ module m_tristan_gpu_3d
        integer(c_int32_t), value :: kind, idx, idy, idz
        type(c_ptr), value :: num, den
      end function
+     integer(c_int) function tg_spectrum_x_bins(ctx, nbins) bind(C, name="tg_spectrum_x_bins")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), intent(out) :: nbins
+     end function
+     integer(c_int) function tg_spectrum_x(ctx, gambins, si, se, sir, ser, xgamma, xslice, grange) &
+         bind(C, name="tg_spectrum_x")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: gambins
+       type(c_ptr), value :: si, se, sir, ser, xgamma, xslice, grange
+     end function
   end interface
 
   type, bind(C) :: tg_restart_meta
@@ -214,7 +226,7 @@ module m_tristan_gpu_3d
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
             gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
             gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
-            gpu_write_restart, gpu_read_restart, gpu_meanq
+            gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum
 
 contains
 
@@ -358,6 +370,27 @@ contains
     real, target, intent(out) :: num(:,:,:), den(:,:,:)
     call check(tg_moments(ctx, int(kind, c_int32_t), 2_c_int32_t, 2_c_int32_t, merge(0_c_int32_t, 2_c_int32_t, mz == 1), &
                c_loc(num), c_loc(den)), "meanq_fld_cur")
+  end subroutine
+
+  ! save_spectrum's arrays from the device (code/output.F90:380-785): nbins
+  ! x slices, specp / spece and the flow-frame specprest / specerest
+  ! (nbins, gambins), each divided by gamma - 1, xgamma, xslice, gmin, gmax;
+  ! the HDF5 write stays the reference's
+  integer function gpu_spectrum_bins()
+    integer(c_int32_t) :: nb
+    call check(tg_spectrum_x_bins(ctx, nb), "tg_spectrum_x_bins")
+    gpu_spectrum_bins = nb
+  end function
+
+  subroutine gpu_spectrum(gambins, specp, spece, specprest, specerest, xgamma, xslice, gmin, gmax)
+    integer, intent(in) :: gambins
+    real, target, intent(out) :: specp(:,:), spece(:,:), specprest(:,:), specerest(:,:), xgamma(:), xslice(:)
+    real, intent(out) :: gmin, gmax
+    real, target :: gr(2)
+    call check(tg_spectrum_x(ctx, int(gambins, c_int32_t), c_loc(specp), c_loc(spece), c_loc(specprest), &
+               c_loc(specerest), c_loc(xgamma), c_loc(xslice), c_loc(gr)), "save_spectrum")
+    gmin = gr(1)
+    gmax = gr(2)
   end subroutine
 
   ! the whole periodic lap fused on the device (replaces lines 115-303)

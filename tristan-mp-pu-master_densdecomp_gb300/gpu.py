@@ -121,7 +121,8 @@ ENTRY_POINTS = (
     "tg_ens_sync_from_host", "tg_ens_sync_to_host", "tg_ens_step", "tg_ens_step_timed", "tg_ens_diag_fp64",
     "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
     "tg_shock_init", "tg_shock_get", "tg_inject_region", "tg_particle_bc", "tg_field_bc", "tg_inject",
-    "tg_write_restart", "tg_read_restart", "tg_moments", "tg_spectrum_dims", "tg_spectrum",
+    "tg_write_restart", "tg_read_restart", "tg_moments", "tg_spectrum_dims", "tg_spectrum", "tg_spectrum_x_bins",
+    "tg_spectrum_x",
 )
 # grid moments of meanq_fld_cur (code/output.F90:5222-5482), by the reference's names
 MOMENTS = ("tdens", "idens", "tbetx", "tbety", "tbetz", "ibetx", "ibety", "ibetz", "tmomx", "tmomy", "tmomz",
@@ -198,6 +199,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_spectrum_dims.restype = ctypes.c_int
     lib.tg_spectrum.argtypes = [P, ctypes.c_int32] + [P] * 6
     lib.tg_spectrum.restype = ctypes.c_int
+    lib.tg_spectrum_x_bins.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
+    lib.tg_spectrum_x_bins.restype = ctypes.c_int
+    lib.tg_spectrum_x.argtypes = [P, ctypes.c_int32] + [P] * 7
+    lib.tg_spectrum_x.restype = ctypes.c_int
     lib.tg_moments.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, P, P]
     lib.tg_moments.restype = ctypes.c_int
     lib.tg_write_restart.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(tg_restart_meta)]
@@ -541,6 +546,20 @@ class GpuSim:
         self._check(self.lib.tg_spectrum(self.h, gambins, si.ctypes.data, se.ctypes.data, xg.ctypes.data,
                                          xs.ctypes.data, ys.ctypes.data, gr.ctypes.data))
         return dict(ions=si, lecs=se, xgamma=xg, xslice=xs, yslice=ys, gammin=float(gr[0]), gammax=float(gr[1]))
+
+    def spectrum_x(self, gambins: int = 200) -> dict:
+        """lab-frame and flow-frame energy spectra per x slice, divided by
+        gamma - 1 (save_spectrum)"""
+        nb = ctypes.c_int32()
+        self._check(self.lib.tg_spectrum_x_bins(self.h, ctypes.byref(nb)))
+        out = {k: np.zeros((gambins, nb.value), np.float32) for k in ("ions", "lecs", "ions_rest", "lecs_rest")}
+        xg = np.zeros(gambins, np.float32)
+        xs = np.zeros(nb.value, np.float32)
+        gr = np.zeros(2, np.float32)
+        self._check(self.lib.tg_spectrum_x(self.h, gambins, out["ions"].ctypes.data, out["lecs"].ctypes.data,
+                                           out["ions_rest"].ctypes.data, out["lecs_rest"].ctypes.data,
+                                           xg.ctypes.data, xs.ctypes.data, gr.ctypes.data))
+        return dict(out, xgamma=xg, xslice=xs, gammin=float(gr[0]), gammax=float(gr[1]))
 
     # -- restart files (write_restart / restart) -------------------------------
     def write_restart(self, fields_path: str, particles_path: str, **meta) -> None:
