@@ -174,6 +174,16 @@ def committed_traffic(workload, form):
         return None
 
 
+def committed_instructions(workload, form):
+    """warp instructions per launch of the tile kernel from the committed ncu summary"""
+    try:
+        with open(os.path.join(ROOT, "profiles", "tile_kernel_traffic.json")) as f:
+            d = json.load(f)
+        return d.get("warp_instructions", {}).get(workload, {}).get(form)
+    except Exception:
+        return None
+
+
 def tile_kernel_bytes(cfg, n_particles, fixed):
     """algorithmic bytes of one push+deposit launch: per particle read
     cell+offsets+u+ch (32 B) and write cell+offsets+u (28 B); per cell the
@@ -451,6 +461,15 @@ def main():
                 "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
                 "traffic": committed_traffic(args.workload, "fp32"),
                 "algorithmic_bytes_per_launch": alg, "launch_ms": phases["particles"]}
+    # the bound the kernel actually sits at: instruction issue (one warp
+    # instruction per clock per SM sub-partition, 4 per SM, at the SM clock
+    # sampled during the timed laps)
+    ninst = committed_instructions(args.workload, "fp32")
+    if ninst and t_kernel > 0 and clk and clk.get("sm_mhz"):
+        issue_peak = 152 * 4 * clk["sm_mhz"] * 1e6
+        roofline["issue"] = {"achieved": ninst / t_kernel, "peak": issue_peak, "unit": "warp-instructions/s",
+                             "frac": ninst / t_kernel / issue_peak, "instructions_per_launch": ninst,
+                             "peak_basis": "152 SMs x 4 issue slots x median SM clock under load"}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         dt_cpu, cores = cpu_baseline(cfg, ions, lecs, args.cpu_steps)
