@@ -346,6 +346,33 @@ int tg_read_restart(tg_ctx *ctx, const char *fields_path, const char *particles_
 #define TG_MOMENT_KINDS 16
 int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz, float *num, float *den);
 
+/* One variable of the .tot. field output (output_tot,
+   code/output.F90:2494-3884) sampled on the device every istep nodes: from
+   the first to the last node i in [1, mx] with (i + mxcum) divisible by
+   istep, likewise in y and (3D) z; tg_output_dims gives the counts
+   (2D: dims[2] = 1). var: TG_OUT_EX..TG_OUT_BZ interpolate the staggered
+   field to the node as interpolfld (code/output.F90:4995-5127) does and add
+   the constant external field when it is on; TG_OUT_JX..TG_OUT_JZ sample
+   the current as it is (the lap's filtered current; the reference re-reads
+   a copy it saved); TG_OUT_MOMENT + TG_MOMENT_* sample meanq_fld_cur's
+   moment with box half-widths idx, idy, idz as tg_moments (dens = TDENS,
+   densi = IDENS, v3x..v3z = TBETX..TBETZ, v3xi.. = IBETX.., v4x.. =
+   TMOMX.., v4xi.. = IMOMX.., keni = IENER; the reference's ken asks for
+   "tener", a name meanq_fld_cur does not know, and so writes zeros). out
+   receives dims[0]*dims[1]*dims[2] floats, x fastest. Synchronises. */
+#define TG_OUT_EX 0
+#define TG_OUT_EY 1
+#define TG_OUT_EZ 2
+#define TG_OUT_BX 3
+#define TG_OUT_BY 4
+#define TG_OUT_BZ 5
+#define TG_OUT_JX 6
+#define TG_OUT_JY 7
+#define TG_OUT_JZ 8
+#define TG_OUT_MOMENT 16
+int tg_output_dims(tg_ctx *ctx, int32_t istep, int32_t *dims);
+int tg_output_var(tg_ctx *ctx, int32_t var, int32_t istep, int32_t idx, int32_t idy, int32_t idz, float *out);
+
 /* Energy spectra in the local flow frame for the spectrum output
    (save_spectrum_2d, code/output.F90:794-1249): slices of 30 cells over
    x in [mx0/2 - 1200, mx0/2 + 400] and the interior in y; the gamma range

@@ -159,6 +159,10 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_spectrum_2d.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 5 + \
                 [ctypes.POINTER(ctypes.c_float)] * 2
             lib.to_spectrum_2d.restype = None
+            lib.to_output_dims.argtypes = [P, ctypes.c_int, ctypes.c_void_p]
+            lib.to_output_dims.restype = ctypes.c_int
+            lib.to_output_var.argtypes = [P] + [ctypes.c_int] * 5 + [ctypes.c_void_p]
+            lib.to_output_var.restype = ctypes.c_int
             lib.to_spectrum_x_bins.argtypes = [P]
             lib.to_spectrum_x_bins.restype = ctypes.c_int
             lib.to_spectrum_x.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 6 + \
@@ -323,6 +327,14 @@ class OracleSim:
         self.lib.to_spectrum_2d(self.ptr, gambins, si.ctypes.data, se.ctypes.data, xg.ctypes.data, xs.ctypes.data,
                                 ys.ctypes.data, ctypes.byref(gmin), ctypes.byref(gmax))
         return dict(ions=si, lecs=se, xgamma=xg, xslice=xs, yslice=ys, gammin=gmin.value, gammax=gmax.value)
+
+    def output_var(self, var: int, istep: int, idx: int = 2, idy: int = 2, idz: int = 2) -> np.ndarray:
+        """output_tot: one variable sampled every istep nodes, (nz, ny, nx)"""
+        dims = np.zeros(3, np.int32)
+        self.lib.to_output_dims(self.ptr, istep, dims.ctypes.data)
+        out = np.zeros(int(dims.prod()), np.float32)
+        self.lib.to_output_var(self.ptr, var, istep, idx, idy, idz if self.cfg.dims == 3 else 0, out.ctypes.data)
+        return out.reshape(dims[2], dims[1], dims[0])
 
     def spectrum_x(self, gambins: int = 200) -> dict:
         """save_spectrum: per x slice, lab-frame and flow-frame spectra"""

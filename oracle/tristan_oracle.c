@@ -1799,3 +1799,133 @@ void to_spectrum_2d(const to_state *s, int gambins, float *spec_i, float *spec_e
     *gmin_out = gammin;
     *gmax_out = gammax;
 }
+
+/* ------------------------------------------------------------------------
+ * output_tot (code/output.F90:2494-3884): one .tot. variable sampled every
+ * istep nodes; E and B through interpolfld (code/output.F90:4995-5127).
+ * --------------------------------------------------------------------- */
+static void to_out_axis(int m, int64_t cum, int istep, int *start, int *n)
+{
+    int s = 1, f = m;
+    while (s <= m && (((s + cum) % istep) + istep) % istep != 0) s++;
+    while (f >= 1 && (((f + cum) % istep) + istep) % istep != 0) f--;
+    *start = s;
+    *n = f >= s ? (f - s) / istep + 1 : 0;
+}
+
+int to_output_dims(const to_state *s, int istep, int *dims)
+{
+    int st;
+    to_out_axis(s->mx, s->mxcum, istep, &st, &dims[0]);
+    to_out_axis(s->my, s->mycum, istep, &st, &dims[1]);
+    if (s->dims == 3) to_out_axis(s->mz, s->mzcum, istep, &st, &dims[2]);
+    else dims[2] = 1;
+    return dims[0] * dims[1] * dims[2];
+}
+
+/* interpolfld for one component: a(l + o) with l the reference's 1-based
+   linear index of the (clamped) node */
+static float to_interpolfld(const to_state *s, int comp, const float *a, float x, float y, float z)
+{
+    int i = (int)x, j = (int)y, k = (int)z;
+    float dx = x - (float)i, dy = y - (float)j, dz = z - (float)k;
+    if (i == 1) i = 2;
+    if (i == s->mx) i = s->mx - 1;
+    if (j == 1) j = 2;
+    if (j == s->my) j = s->my - 1;
+    if (k == 1) k = 2;
+    if (k == s->mz) k = s->mz - 1;
+    int64_t ix = 1, iy = s->mx, iz = (int64_t)s->mx * s->my;
+    if (s->dims == 2) {
+        k = 1;
+        dz = 0.0f;
+        iz = 0;
+    }
+    const float *L = a + (i - 1) + iy * (j - 1) + iz * (k - 1);
+#define A(o) L[(o)]
+    float f, g;
+    if (comp == 0) {
+        f = A(0) + A(-ix) + dx * (A(ix) - A(-ix));
+        f = f + dy * (A(iy) + A(-ix + iy) + dx * (A(ix + iy) - A(-ix + iy)) - f);
+        g = A(iz) + A(-ix + iz) + dx * (A(ix + iz) - A(-ix + iz));
+        g = g + dy * (A(iy + iz) + A(-ix + iy + iz) + dx * (A(ix + iy + iz) - A(-ix + iy + iz)) - g);
+        return (f + dz * (g - f)) * 0.5f;
+    }
+    if (comp == 1) {
+        f = A(0) + A(-iy) + dy * (A(iy) - A(-iy));
+        f = f + dz * (A(iz) + A(-iy + iz) + dy * (A(iy + iz) - A(-iy + iz)) - f);
+        g = A(ix) + A(-iy + ix) + dy * (A(iy + ix) - A(-iy + ix));
+        g = g + dz * (A(iz + ix) + A(-iy + iz + ix) + dy * (A(iy + iz + ix) - A(-iy + iz + ix)) - g);
+        return (f + dx * (g - f)) * 0.5f;
+    }
+    if (comp == 2) {
+        f = A(0) + A(-iz) + dz * (A(iz) - A(-iz));
+        f = f + dx * (A(ix) + A(-iz + ix) + dz * (A(iz + ix) - A(-iz + ix)) - f);
+        g = A(iy) + A(-iz + iy) + dz * (A(iz + iy) - A(-iz + iy));
+        g = g + dx * (A(ix + iy) + A(-iz + ix + iy) + dz * (A(iz + ix + iy) - A(-iz + ix + iy)) - g);
+        return (f + dy * (g - f)) * 0.5f;
+    }
+    if (comp == 3) {
+        f = A(-iy) + A(-iy - iz) + dz * (A(-iy + iz) - A(-iy - iz));
+        f = A(0) + A(-iz) + dz * (A(iz) - A(-iz)) + f + dy * (A(iy) + A(iy - iz) + dz * (A(iy + iz) - A(iy - iz)) - f);
+        g = A(ix - iy) + A(ix - iy - iz) + dz * (A(ix - iy + iz) - A(ix - iy - iz));
+        g = A(ix) + A(ix - iz) + dz * (A(ix + iz) - A(ix - iz)) + g +
+            dy * (A(ix + iy) + A(ix + iy - iz) + dz * (A(ix + iy + iz) - A(ix + iy - iz)) - g);
+        return (f + dx * (g - f)) * 0.25f;
+    }
+    if (comp == 4) {
+        f = A(-iz) + A(-iz - ix) + dx * (A(-iz + ix) - A(-iz - ix));
+        f = A(0) + A(-ix) + dx * (A(ix) - A(-ix)) + f + dz * (A(iz) + A(iz - ix) + dx * (A(iz + ix) - A(iz - ix)) - f);
+        g = A(iy - iz) + A(iy - iz - ix) + dx * (A(iy - iz + ix) - A(iy - iz - ix));
+        g = A(iy) + A(iy - ix) + dx * (A(iy + ix) - A(iy - ix)) + g +
+            dz * (A(iy + iz) + A(iy + iz - ix) + dx * (A(iy + iz + ix) - A(iy + iz - ix)) - g);
+        return (f + dy * (g - f)) * 0.25f;
+    }
+    f = A(-ix) + A(-ix - iy) + dy * (A(-ix + iy) - A(-ix - iy));
+    f = A(0) + A(-iy) + dy * (A(iy) - A(-iy)) + f + dx * (A(ix) + A(ix - iy) + dy * (A(ix + iy) - A(ix - iy)) - f);
+    g = A(iz - ix) + A(iz - ix - iy) + dy * (A(iz - ix + iy) - A(iz - ix - iy));
+    g = A(iz) + A(iz - iy) + dy * (A(iz + iy) - A(iz - iy)) + g +
+        dx * (A(iz + ix) + A(iz + ix - iy) + dy * (A(iz + ix + iy) - A(iz + ix - iy)) - g);
+    return (f + dz * (g - f)) * 0.25f;
+#undef A
+}
+
+/* var: 0-5 E, B; 6-8 currents; 16 + k the meanq_fld_cur moment k */
+int to_output_var(to_state *s, int var, int istep, int idx, int idy, int idz, float *out)
+{
+    int st[3], n[3];
+    to_out_axis(s->mx, s->mxcum, istep, &st[0], &n[0]);
+    to_out_axis(s->my, s->mycum, istep, &st[1], &n[1]);
+    if (s->dims == 3) to_out_axis(s->mz, s->mzcum, istep, &st[2], &n[2]);
+    else {
+        st[2] = 1;
+        n[2] = 1;
+    }
+    const int64_t lot = to_lot(s);
+    float *num = NULL, *den = NULL;
+    const float *src;
+    float *arrs[9] = {s->ex, s->ey, s->ez, s->bx, s->by, s->bz, s->curx, s->cury, s->curz};
+    if (var >= 16) {
+        num = malloc(sizeof(float) * lot);
+        den = malloc(sizeof(float) * lot);
+        to_meanq(s, var - 16, idx, idy, idz, num, den);
+        src = num;
+    } else {
+        src = arrs[var];
+    }
+    int64_t t = 0;
+    for (int c = 0; c < n[2]; c++)
+        for (int b = 0; b < n[1]; b++)
+            for (int a = 0; a < n[0]; a++, t++) {
+                const int i = st[0] + istep * a, j = st[1] + istep * b, k = s->dims == 3 ? st[2] + istep * c : 1;
+                if (var < 6) {
+                    const float e = s->external_fields ? s->ext[var] : 0.0f;
+                    out[t] = to_interpolfld(s, var, src, (float)i, (float)j, (float)k) + e;
+                } else {
+                    out[t] = src[(i - 1) + (int64_t)s->mx * (j - 1) + (int64_t)s->mx * s->my * (k - 1)];
+                }
+            }
+    free(num);
+    free(den);
+    return (int)t;
+}

@@ -206,6 +206,10 @@ void to_step_shock(to_state *s, to_shock *k);
    imomy imomz eener iener; num receives the moment, den the box-averaged
    weight (both mx*my*mz); the current arrays are left as they were */
 void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, float *den);
+/* output_tot (code/output.F90:2494-3884): the istep-sampled counts, and one
+   variable (0-5 E/B through interpolfld, 6-8 currents, 16 + k moment k) */
+int to_output_dims(const to_state *s, int istep, int *dims);
+int to_output_var(to_state *s, int var, int istep, int idx, int idy, int idz, float *out);
 /* flow-frame energy spectra per slice (save_spectrum_2d,
    code/output.F90:794-1249); dims from to_spectrum_dims */
 float to_log10f(float x);

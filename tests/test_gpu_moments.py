@@ -126,3 +126,39 @@ def test_x_slice_spectra_match_oracle():
         assert abs(rest_g.sum() - rest_o.sum()) <= 1e-5 * tot + 2
         assert np.abs(rest_g - rest_o).sum() <= max(4.0, 2e-3 * tot), sp
     g.close()
+
+
+@pytest.mark.parametrize("dims,order,ext", [(2, 3, False), (2, 1, True), (3, 2, False)])
+def test_output_tot_matches_oracle(dims, order, ext):
+    """output_tot's variables sampled on the device: E and B through
+    interpolfld (plus the constant external field), the currents and the
+    moments, at istep 2 and 3 (the sampled range then starts and ends
+    inside the array). Fields and currents bit-exact, densities exact,
+    velocity moments within 1e-5"""
+    from tristan_gb300.gpu import MOMENTS, GpuSim
+    kw = dict(external_fields=1, ext=(0.0, 0.0, 0.0, 0.0, 0.0, 0.05)) if ext else {}
+    cfg = small_cfg(dims, order, fixed=1, **kw)
+    ions, lecs = beams(cfg)
+    f = random_fields(cfg, np.random.default_rng(6), scale=0.02)
+    o = oracle.OracleSim(cfg)
+    for k, v in f.items():
+        o.fields[k][:] = v
+    o.set_particles(ions, lecs)
+    g = GpuSim(cfg)
+    g.set_fields(**f)
+    g.sync_from_host()
+    g.set_particles(ions, lecs)
+    g.step(3)
+    o.step(3)
+    for istep in (2, 3):
+        for name, code in GpuSim.OUTPUT_VARS.items():
+            a, b = g.output_var(name, istep), o.output_var(code, istep)
+            assert a.shape == b.shape and a.size > 0
+            np.testing.assert_array_equal(a, b, err_msg=f"{name} istep {istep}")
+        for name in ("tdens", "idens"):
+            np.testing.assert_array_equal(g.output_var(name, istep), o.output_var(16 + MOMENTS.index(name), istep),
+                                          err_msg=name)
+        for name in ("tbetx", "imomy", "iener"):
+            a, b = g.output_var(name, istep), o.output_var(16 + MOMENTS.index(name), istep)
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6 * max(np.abs(b).max(), 1e-30), err_msg=name)
+    g.close()

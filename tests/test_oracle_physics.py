@@ -139,3 +139,35 @@ def test_x_slice_spectrum_weights_and_axes():
         lab = (s[sp] * xg).sum()
         assert abs(lab - w[inside].sum()) <= 1.0 + 1e-5 * lab, sp
         assert abs((s[sp + "_rest"] * xg).sum() - lab) <= 0.01 * lab, sp
+
+
+def test_output_tot_node_interpolation_known_answer():
+    """at the output nodes (integer positions) interpolfld's weights vanish:
+    ex is the mean of its two x neighbours and, in 2D, bz the mean of its
+    four (x, y) neighbours, summed in the reference's order; currents are
+    sampled as they are"""
+    from test_gpu_parity import beams, random_fields, small_cfg
+    cfg = small_cfg(2, 3, fixed=1)
+    ions, lecs = beams(cfg)
+    o = oracle.OracleSim(cfg)
+    o.set_particles(ions, lecs)
+    f = random_fields(cfg, np.random.default_rng(7), scale=0.02,
+                      names=("ex", "ey", "ez", "bx", "by", "bz", "curx"))
+    for k, v in f.items():
+        o.fields[k][:] = v
+    mx, my = cfg.mx, cfg.my
+    ex = o.fields["ex"].reshape(my, mx)
+    bz = o.fields["bz"].reshape(my, mx)
+    cx = o.fields["curx"].reshape(my, mx).copy()
+    for istep in (2, 3):
+        i = np.arange(istep, mx + 1, istep)
+        j = np.arange(istep, my + 1, istep)
+        ic = np.clip(i, 2, mx - 1) - 1  # 0-based, clamped as interpolfld
+        jc = np.clip(j, 2, my - 1) - 1
+        J, I = np.meshgrid(jc, ic, indexing="ij")
+        want_ex = (ex[J, I] + ex[J, I - 1]) * np.float32(0.5)
+        want_bz = (((bz[J, I] + bz[J - 1, I]) + np.float32(0.0)) + (bz[J, I - 1] + bz[J - 1, I - 1])) * np.float32(0.25)
+        np.testing.assert_array_equal(o.output_var(0, istep)[0], want_ex)
+        np.testing.assert_array_equal(o.output_var(5, istep)[0], want_bz)
+        Jr, Ir = np.meshgrid(j - 1, i - 1, indexing="ij")
+        np.testing.assert_array_equal(o.output_var(6, istep)[0], cx[Jr, Ir])

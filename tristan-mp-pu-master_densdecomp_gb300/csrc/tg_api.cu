@@ -1643,6 +1643,90 @@ extern "C" int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, i
 }
 
 // ---------------------------------------------------------------------------
+// output_tot (code/output.F90:2494-3884): the .tot. variables sampled every
+// istep nodes
+// ---------------------------------------------------------------------------
+// first and last node in [1, m] with (node + cum) divisible by istep (the
+// reference's start/finish adjustment loops), and the count
+static void out_axis(int m, long long cum, int istep, int &start, int &n) {
+    auto md = [&](long long a) { return ((a % istep) + istep) % istep; };
+    int s = 1, f = m;
+    while (s <= m && md(s + cum) != 0) s++;
+    while (f >= 1 && md(f + cum) != 0) f--;
+    start = s;
+    n = f >= s ? (f - s) / istep + 1 : 0;
+}
+
+static void out_grid(const tg_ctx *ctx, int istep, int start[3], int n[3]) {
+    const Geom &g = ctx->g;
+    out_axis(g.mx, ctx->P.mxcum, istep, start[0], n[0]);
+    out_axis(g.my, ctx->P.mycum, istep, start[1], n[1]);
+    if (g.dims == 3) out_axis(g.mz, ctx->P.mzcum, istep, start[2], n[2]);
+    else {
+        start[2] = 1;
+        n[2] = 1;
+    }
+}
+
+extern "C" int tg_output_dims(tg_ctx *ctx, int32_t istep, int32_t *dims) {
+    if (!ctx || !dims || istep < 1) return TG_ERR_ARG;
+    int start[3], n[3];
+    out_grid(ctx, istep, start, n);
+    for (int a = 0; a < 3; a++) dims[a] = n[a];
+    return TG_OK;
+}
+
+extern "C" int tg_output_var(tg_ctx *ctx, int32_t var, int32_t istep, int32_t idx, int32_t idy, int32_t idz,
+                             float *out) {
+    if (!ctx || !out || istep < 1) return TG_ERR_ARG;
+    const bool moment = var >= TG_OUT_MOMENT && var < TG_OUT_MOMENT + TG_MOMENT_KINDS;
+    if (!(var >= TG_OUT_EX && var <= TG_OUT_JZ) && !moment)
+        return fail(ctx, TG_ERR_ARG, "tg_output_var: variable %d unknown", var);
+    if (moment && (idx < 0 || idy < 0 || idz < 0))
+        return fail(ctx, TG_ERR_ARG, "tg_output_var: negative box half-width");
+    int start[3], n[3];
+    out_grid(ctx, istep, start, n);
+    const size_t total = (size_t)n[0] * n[1] * n[2];
+    if (total == 0) return TG_OK;
+    const size_t lot = (size_t)ctx->g.lot;
+    const float *src;
+    int comp = -1;
+    float add = 0.0f;
+    if (moment) {
+        if (!ctx->mom[0]) {
+            int r = dalloc(ctx, &ctx->mom[0], lot);
+            if (!r) r = dalloc(ctx, &ctx->mom[1], lot);
+            if (r) return r;
+            CK(cudaMemsetAsync(ctx->mom[0], 0, lot * 8, ctx->st));
+            CK(cudaMemsetAsync(ctx->mom[1], 0, lot * 8, ctx->st));
+        }
+        long long cnt[2];
+        int r = exact_counts(ctx, cnt);
+        if (r) return r;
+        float *f3[3] = {ctx->ftmp[0], ctx->ftmp[1], ctx->ftmp[2]};
+        CK(launch_moments(ctx->g, ctx->P, ctx->sp[ctx->par], ctx->d_cnt + 2 * ctx->par, cnt[0] + cnt[1],
+                          var - TG_OUT_MOMENT, idx, idy, ctx->g.dims == 3 ? idz : 0, ctx->mom[0], ctx->mom[1], f3,
+                          ctx->st));
+        src = f3[0];
+    } else if (var <= TG_OUT_BZ) {
+        comp = var - TG_OUT_EX;
+        src = ctx->f[comp];
+        // get_external_fields' constant values (zero when off)
+        add = ctx->P.external_fields ? ctx->P.ext[comp] : 0.0f;
+    } else {
+        src = ctx->f[6 + (var - TG_OUT_JX)];
+    }
+    float *d_out = nullptr;
+    CK(cudaMalloc(&d_out, total * 4));
+    cudaError_t e = launch_output_sample(ctx->g, comp, src, add, start, n, istep, d_out, ctx->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, total * 4, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_output_var: %s", cudaGetErrorString(e));
+    return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------
 // flow-frame energy spectra (save_spectrum_2d, code/output.F90:794-1249)
 // ---------------------------------------------------------------------------
 extern "C" int tg_spectrum_dims(tg_ctx *ctx, int32_t gambins, int32_t *nxbins, int32_t *nybins) {

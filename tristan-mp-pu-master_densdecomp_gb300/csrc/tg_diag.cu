@@ -319,6 +319,109 @@ cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, co
 }
 
 // ---------------------------------------------------------------------------
+// output_tot (code/output.F90:2494-3884): one variable of the .tot. field
+// file sampled every istep nodes. E and B go through interpolfld
+// (code/output.F90:4995-5127): each staggered component averaged to the node
+// and tri-linearly interpolated at (x, y, z), in the reference's order of
+// operations; the output nodes are integer positions, so the interpolation
+// weights are zero, but the expressions are kept whole so that the roundings
+// (signed zeros included) are the reference's.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__device__ __forceinline__ float interpolfld_one(const Geom &g, int comp, const float *__restrict__ a, float x,
+                                                 float y, float z) {
+    int i = (int)x, j = (int)y, k = DIM == 3 ? (int)z : 1;
+    const float dx = x - (float)i, dy = y - (float)j;
+    float dz = DIM == 3 ? z - (float)k : 0.0f;
+    if (i == 1) i = 2;
+    if (i == g.mx) i = g.mx - 1;
+    if (j == 1) j = 2;
+    if (j == g.my) j = g.my - 1;
+    if (DIM == 3) {
+        if (k == 1) k = 2;
+        if (k == g.mz) k = g.mz - 1;
+    }
+    const long long ix = 1, iy = g.sy, iz = DIM == 3 ? g.sz : 0;
+    // Fortran's 1-based l = i + iy (j - 1) + iz (k - 1) as a 0-based pointer
+    const float *A = a + (i - 1) + iy * (j - 1) + iz * (k - 1);
+    auto f_ = [&](long long o) { return A[o]; };
+    float f, h;
+    switch (comp) {
+    case 0:  // ex: half-integer in x
+        f = f_(0) + f_(-ix) + dx * (f_(ix) - f_(-ix));
+        f = f + dy * (f_(iy) + f_(-ix + iy) + dx * (f_(ix + iy) - f_(-ix + iy)) - f);
+        h = f_(iz) + f_(-ix + iz) + dx * (f_(ix + iz) - f_(-ix + iz));
+        h = h + dy * (f_(iy + iz) + f_(-ix + iy + iz) + dx * (f_(ix + iy + iz) - f_(-ix + iy + iz)) - h);
+        return (f + dz * (h - f)) * 0.5f;
+    case 1:  // ey
+        f = f_(0) + f_(-iy) + dy * (f_(iy) - f_(-iy));
+        f = f + dz * (f_(iz) + f_(-iy + iz) + dy * (f_(iy + iz) - f_(-iy + iz)) - f);
+        h = f_(ix) + f_(-iy + ix) + dy * (f_(iy + ix) - f_(-iy + ix));
+        h = h + dz * (f_(iz + ix) + f_(-iy + iz + ix) + dy * (f_(iy + iz + ix) - f_(-iy + iz + ix)) - h);
+        return (f + dx * (h - f)) * 0.5f;
+    case 2:  // ez
+        f = f_(0) + f_(-iz) + dz * (f_(iz) - f_(-iz));
+        f = f + dx * (f_(ix) + f_(-iz + ix) + dz * (f_(iz + ix) - f_(-iz + ix)) - f);
+        h = f_(iy) + f_(-iz + iy) + dz * (f_(iz + iy) - f_(-iz + iy));
+        h = h + dx * (f_(ix + iy) + f_(-iz + ix + iy) + dz * (f_(iz + ix + iy) - f_(-iz + ix + iy)) - h);
+        return (f + dy * (h - f)) * 0.5f;
+    case 3:  // bx: half-integer in y and z
+        f = f_(-iy) + f_(-iy - iz) + dz * (f_(-iy + iz) - f_(-iy - iz));
+        f = f_(0) + f_(-iz) + dz * (f_(iz) - f_(-iz)) + f +
+            dy * (f_(iy) + f_(iy - iz) + dz * (f_(iy + iz) - f_(iy - iz)) - f);
+        h = f_(ix - iy) + f_(ix - iy - iz) + dz * (f_(ix - iy + iz) - f_(ix - iy - iz));
+        h = f_(ix) + f_(ix - iz) + dz * (f_(ix + iz) - f_(ix - iz)) + h +
+            dy * (f_(ix + iy) + f_(ix + iy - iz) + dz * (f_(ix + iy + iz) - f_(ix + iy - iz)) - h);
+        return (f + dx * (h - f)) * 0.25f;
+    case 4:  // by
+        f = f_(-iz) + f_(-iz - ix) + dx * (f_(-iz + ix) - f_(-iz - ix));
+        f = f_(0) + f_(-ix) + dx * (f_(ix) - f_(-ix)) + f +
+            dz * (f_(iz) + f_(iz - ix) + dx * (f_(iz + ix) - f_(iz - ix)) - f);
+        h = f_(iy - iz) + f_(iy - iz - ix) + dx * (f_(iy - iz + ix) - f_(iy - iz - ix));
+        h = f_(iy) + f_(iy - ix) + dx * (f_(iy + ix) - f_(iy - ix)) + h +
+            dz * (f_(iy + iz) + f_(iy + iz - ix) + dx * (f_(iy + iz + ix) - f_(iy + iz - ix)) - h);
+        return (f + dy * (h - f)) * 0.25f;
+    default:  // bz
+        f = f_(-ix) + f_(-ix - iy) + dy * (f_(-ix + iy) - f_(-ix - iy));
+        f = f_(0) + f_(-iy) + dy * (f_(iy) - f_(-iy)) + f +
+            dx * (f_(ix) + f_(ix - iy) + dy * (f_(ix + iy) - f_(ix - iy)) - f);
+        h = f_(iz - ix) + f_(iz - ix - iy) + dy * (f_(iz - ix + iy) - f_(iz - ix - iy));
+        h = f_(iz) + f_(iz - iy) + dy * (f_(iz + iy) - f_(iz - iy)) + h +
+            dx * (f_(iz + ix) + f_(iz + ix - iy) + dy * (f_(iz + ix + iy) - f_(iz + ix - iy)) - h);
+        return (f + dz * (h - f)) * 0.25f;
+    }
+}
+
+// out[a + n0 (b + n1 c)] = variable at node (start + istep (a, b, c)):
+// comp 0-5 interpolated E / B plus the constant external field add, comp < 0
+// the array's value at the node
+template <int DIM>
+__global__ void __launch_bounds__(256) k_output_sample(Geom g, int comp, const float *__restrict__ a, float add,
+                                                       int3 start, int3 n, int istep, float *out) {
+    const long long total = (long long)n.x * n.y * n.z;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int ax = (int)(t % n.x), r = (int)(t / n.x);
+        const int by = r % n.y, cz = r / n.y;
+        const int i = start.x + istep * ax, j = start.y + istep * by, k = DIM == 3 ? start.z + istep * cz : 1;
+        float v;
+        if (comp >= 0) v = interpolfld_one<DIM>(g, comp, a, (float)i, (float)j, (float)k) + add;
+        else v = a[(i - 1) + g.sy * (j - 1) + g.sz * (k - 1)];
+        out[t] = v;
+    }
+}
+
+cudaError_t launch_output_sample(const Geom &g, int comp, const float *a, float add, const int start[3],
+                                 const int n[3], int istep, float *out, cudaStream_t st) {
+    const long long total = (long long)n[0] * n[1] * n[2];
+    if (total <= 0) return cudaSuccess;
+    const int3 s3 = make_int3(start[0], start[1], start[2]), n3 = make_int3(n[0], n[1], n[2]);
+    if (g.dims == 3) k_output_sample<3><<<dgrid(total), 256, 0, st>>>(g, comp, a, add, s3, n3, istep, out);
+    else k_output_sample<2><<<dgrid(total), 256, 0, st>>>(g, comp, a, add, s3, n3, istep, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // flow-frame energy spectra per slice (save_spectrum_2d,
 // code/output.F90:794-1249)
 // ---------------------------------------------------------------------------

@@ -474,6 +474,10 @@ cudaError_t launch_spec_range(const Species *sp, const long long *count, long lo
 cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &sg, const Species &sp,
                                 const long long *count, long long hint, double *acc, float *mean, float lg0,
                                 float dgam, float *spec, float *spec_lab, cudaStream_t st);
+// output_tot's sampling: comp 0-5 interpolated E / B (plus add), comp < 0
+// the array itself, at nodes start + istep (a, b, c), a < n[0] ... (tg_diag.cu)
+cudaError_t launch_output_sample(const Geom &g, int comp, const float *a, float add, const int start[3],
+                                 const int n[3], int istep, float *out, cudaStream_t st);
 // grid moments (meanq_fld_cur) into f3[0] (moment) and f3[1] (weight);
 // num / den are zeroed FP64 scratch of g.lot cells, left zeroed
 cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,

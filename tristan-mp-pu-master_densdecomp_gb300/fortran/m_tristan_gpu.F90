@@ -194,6 +194,12 @@ module m_tristan_gpu_3d
        integer(c_int32_t), value :: kind, idx, idy, idz
        type(c_ptr), value :: num, den
      end function
+     integer(c_int) function tg_output_var(ctx, var, istep, idx, idy, idz, out) bind(C, name="tg_output_var")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: var, istep, idx, idy, idz
+       type(c_ptr), value :: out
+     end function
      integer(c_int) function tg_spectrum_x_bins(ctx, nbins) bind(C, name="tg_spectrum_x_bins")
        import :: c_int, c_ptr, c_int32_t
        type(c_ptr), value :: ctx
@@ -226,7 +232,7 @@ module m_tristan_gpu_3d
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
             gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
             gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
-            gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum
+            gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum, gpu_output_var
 
 contains
 
@@ -370,6 +376,16 @@ contains
     real, target, intent(out) :: num(:,:,:), den(:,:,:)
     call check(tg_moments(ctx, int(kind, c_int32_t), 2_c_int32_t, 2_c_int32_t, merge(0_c_int32_t, 2_c_int32_t, mz == 1), &
                c_loc(num), c_loc(den)), "meanq_fld_cur")
+  end subroutine
+
+  ! one .tot. variable of output_tot sampled on the device into its
+  ! temporary1(mx1,my1,mz1) array (var: 0-5 ex..bz, 6-8 jx..jz, 16 + the
+  ! meanq_fld_cur kind of tg_moments); the HDF5 write stays the reference's
+  subroutine gpu_output_var(var, istep, out)
+    integer, intent(in) :: var, istep
+    real, target, intent(out) :: out(:,:,:)
+    call check(tg_output_var(ctx, int(var, c_int32_t), int(istep, c_int32_t), 2_c_int32_t, 2_c_int32_t, &
+               merge(0_c_int32_t, 2_c_int32_t, mz == 1), c_loc(out)), "output_tot")
   end subroutine
 
   ! save_spectrum's arrays from the device (code/output.F90:380-785): nbins

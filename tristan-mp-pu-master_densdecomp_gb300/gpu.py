@@ -122,7 +122,7 @@ ENTRY_POINTS = (
     "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
     "tg_shock_init", "tg_shock_get", "tg_inject_region", "tg_particle_bc", "tg_field_bc", "tg_inject",
     "tg_write_restart", "tg_read_restart", "tg_moments", "tg_spectrum_dims", "tg_spectrum", "tg_spectrum_x_bins",
-    "tg_spectrum_x",
+    "tg_spectrum_x", "tg_output_dims", "tg_output_var",
 )
 # grid moments of meanq_fld_cur (code/output.F90:5222-5482), by the reference's names
 MOMENTS = ("tdens", "idens", "tbetx", "tbety", "tbetz", "ibetx", "ibety", "ibetz", "tmomx", "tmomy", "tmomz",
@@ -199,6 +199,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_spectrum_dims.restype = ctypes.c_int
     lib.tg_spectrum.argtypes = [P, ctypes.c_int32] + [P] * 6
     lib.tg_spectrum.restype = ctypes.c_int
+    lib.tg_output_dims.argtypes = [P, ctypes.c_int32, P]
+    lib.tg_output_dims.restype = ctypes.c_int
+    lib.tg_output_var.argtypes = [P] + [ctypes.c_int32] * 5 + [P]
+    lib.tg_output_var.restype = ctypes.c_int
     lib.tg_spectrum_x_bins.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     lib.tg_spectrum_x_bins.restype = ctypes.c_int
     lib.tg_spectrum_x.argtypes = [P, ctypes.c_int32] + [P] * 7
@@ -546,6 +550,21 @@ class GpuSim:
         self._check(self.lib.tg_spectrum(self.h, gambins, si.ctypes.data, se.ctypes.data, xg.ctypes.data,
                                          xs.ctypes.data, ys.ctypes.data, gr.ctypes.data))
         return dict(ions=si, lecs=se, xgamma=xg, xslice=xs, yslice=ys, gammin=float(gr[0]), gammax=float(gr[1]))
+
+    # .tot. output variables (output_tot): E, B, currents, moments by name
+    OUTPUT_VARS = {"ex": 0, "ey": 1, "ez": 2, "bx": 3, "by": 4, "bz": 5, "jx": 6, "jy": 7, "jz": 8}
+
+    def output_var(self, var, istep: int, idx: int = 2, idy: int = 2, idz: int = 2) -> np.ndarray:
+        """one .tot. variable sampled every istep nodes (output_tot), shaped
+        (nz, ny, nx); var: a name of OUTPUT_VARS, a moment name of MOMENTS,
+        or the integer code"""
+        if isinstance(var, str):
+            var = self.OUTPUT_VARS[var] if var in self.OUTPUT_VARS else 16 + MOMENTS.index(var)
+        dims = np.zeros(3, np.int32)
+        self._check(self.lib.tg_output_dims(self.h, istep, dims.ctypes.data))
+        out = np.zeros(int(dims.prod()), np.float32)
+        self._check(self.lib.tg_output_var(self.h, int(var), istep, idx, idy, idz, out.ctypes.data))
+        return out.reshape(dims[2], dims[1], dims[0])
 
     def spectrum_x(self, gambins: int = 200) -> dict:
         """lab-frame and flow-frame energy spectra per x slice, divided by
