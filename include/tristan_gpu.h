@@ -372,6 +372,17 @@ int tg_moments(tg_ctx *ctx, int32_t kind, int32_t idx, int32_t idy, int32_t idz,
 #define TG_OUT_MOMENT 16
 int tg_output_dims(tg_ctx *ctx, int32_t istep, int32_t *dims);
 int tg_output_var(tg_ctx *ctx, int32_t var, int32_t istep, int32_t idx, int32_t idy, int32_t idz, float *out);
+/* The particle sample of output_tot (prtl.tot, code/output.F90:3293-3884):
+   the particles of one species (0 ions, 1 electrons) with
+   modulo(ind / 2, stride) = 0, in the device's order (tile-sorted; the
+   reference writes its array order; the set is the same). Per particle
+   vals[k * cap + i] holds, for k = 0..7, x + mxcum, y + mycum, z + mzcum,
+   u, v, w, ch and gamma = sqrt(1 + (u^2 + v^2 + w^2)) (the reference's
+   xi, yi, zi, ui, vi, wi, chi, gammai), and ids[k * cap + i], k = 0..1,
+   ind and proc. *count receives the number selected; when it exceeds cap
+   only the count is set (cap = 0 sizes the arrays). Synchronises. */
+int tg_output_particles(tg_ctx *ctx, int32_t species, int32_t stride, int64_t cap, float *vals, int32_t *ids,
+                        int64_t *count);
 
 /* Energy spectra in the local flow frame for the spectrum output
    (save_spectrum_2d, code/output.F90:794-1249): slices of 30 cells over

@@ -163,6 +163,9 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_output_dims.restype = ctypes.c_int
             lib.to_output_var.argtypes = [P] + [ctypes.c_int] * 5 + [ctypes.c_void_p]
             lib.to_output_var.restype = ctypes.c_int
+            lib.to_output_particles.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
+                                                ctypes.c_void_p]
+            lib.to_output_particles.restype = ctypes.c_int64
             lib.to_spectrum_x_bins.argtypes = [P]
             lib.to_spectrum_x_bins.restype = ctypes.c_int
             lib.to_spectrum_x.argtypes = [P, ctypes.c_int] + [ctypes.c_void_p] * 6 + \
@@ -335,6 +338,17 @@ class OracleSim:
         out = np.zeros(int(dims.prod()), np.float32)
         self.lib.to_output_var(self.ptr, var, istep, idx, idy, idz if self.cfg.dims == 3 else 0, out.ctypes.data)
         return out.reshape(dims[2], dims[1], dims[0])
+
+    def output_particles(self, species: int, stride: int) -> dict:
+        """output_tot's particle sample: x, y, z, u, v, w, ch, gamma, ind, proc"""
+        total = self.lib.to_output_particles(self.ptr, species, stride, 0, None, None)
+        vals = np.zeros((8, max(total, 1)), np.float32)
+        ids = np.zeros((2, max(total, 1)), np.int32)
+        self.lib.to_output_particles(self.ptr, species, stride, max(total, 1), vals.ctypes.data, ids.ctypes.data)
+        names = ("x", "y", "z", "u", "v", "w", "ch", "gamma")
+        out = {k: vals[i, :total] for i, k in enumerate(names)}
+        out["ind"], out["proc"] = ids[0, :total], ids[1, :total]
+        return out
 
     def spectrum_x(self, gambins: int = 200) -> dict:
         """save_spectrum: per x slice, lab-frame and flow-frame spectra"""

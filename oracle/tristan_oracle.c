@@ -1929,3 +1929,37 @@ int to_output_var(to_state *s, int var, int istep, int idx, int idy, int idz, fl
     free(den);
     return (int)t;
 }
+
+/* output_tot's particle sample (prtl.tot, code/output.F90:3293-3884): the
+   species' particles with modulo(ind / 2, stride) = 0 in array order;
+   vals[k * cap + i] = x + mxcum, y + mycum, z + mzcum, u, v, w, ch, gamma;
+   ids[k * cap + i] = ind, proc. Returns the number selected (vals and ids
+   are written only when it fits in cap). */
+int64_t to_output_particles(const to_state *s, int species, int stride, int64_t cap, float *vals, int32_t *ids)
+{
+    const int64_t base = species == 0 ? 0 : s->maxhlf, cnt = species == 0 ? s->ions : s->lecs;
+    int64_t total = 0;
+    for (int64_t n = 0; n < cnt; n++) {
+        const int h = s->p[base + n].ind / 2;
+        if (((h % stride) + stride) % stride == 0) total++;
+    }
+    if (total > cap) return total;
+    int64_t o = 0;
+    for (int64_t n = 0; n < cnt; n++) {
+        const to_particle *p = &s->p[base + n];
+        const int h = p->ind / 2;
+        if (((h % stride) + stride) % stride != 0) continue;
+        vals[o] = p->x + (float)s->mxcum;
+        vals[cap + o] = p->y + (float)s->mycum;
+        vals[2 * cap + o] = p->z + (float)s->mzcum;
+        vals[3 * cap + o] = p->u;
+        vals[4 * cap + o] = p->v;
+        vals[5 * cap + o] = p->w;
+        vals[6 * cap + o] = p->ch;
+        vals[7 * cap + o] = sqrtf(1.0f + (p->u * p->u + p->v * p->v + p->w * p->w));
+        ids[o] = p->ind;
+        ids[cap + o] = p->proc;
+        o++;
+    }
+    return total;
+}

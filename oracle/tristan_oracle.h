@@ -210,6 +210,9 @@ void to_meanq(to_state *s, int kind, int idx, int idy, int idz, float *num, floa
    variable (0-5 E/B through interpolfld, 6-8 currents, 16 + k moment k) */
 int to_output_dims(const to_state *s, int istep, int *dims);
 int to_output_var(to_state *s, int var, int istep, int idx, int idy, int idz, float *out);
+/* output_tot's particle sample (prtl.tot): selected count; values when it
+   fits in cap */
+int64_t to_output_particles(const to_state *s, int species, int stride, int64_t cap, float *vals, int32_t *ids);
 /* flow-frame energy spectra per slice (save_spectrum_2d,
    code/output.F90:794-1249); dims from to_spectrum_dims */
 float to_log10f(float x);

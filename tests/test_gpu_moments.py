@@ -162,3 +162,33 @@ def test_output_tot_matches_oracle(dims, order, ext):
             a, b = g.output_var(name, istep), o.output_var(16 + MOMENTS.index(name), istep)
             np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6 * max(np.abs(b).max(), 1e-30), err_msg=name)
     g.close()
+
+
+@pytest.mark.parametrize("dims,order", [(2, 3), (3, 2)])
+def test_output_particle_sample_matches_oracle(dims, order):
+    """output_tot's particle sample (prtl.tot) on the device: the same
+    particles (modulo(ind / 2, stride) = 0, compared keyed by ind) with the
+    same values bit for bit; negative ind (beam particles) included"""
+    from tristan_gb300.gpu import GpuSim
+    cfg = small_cfg(dims, order, fixed=1)
+    ions, lecs = beams(cfg)
+    ions["ind"][::5] *= -1
+    f = random_fields(cfg, np.random.default_rng(8), scale=0.02)
+    o = oracle.OracleSim(cfg)
+    for k, v in f.items():
+        o.fields[k][:] = v
+    o.set_particles(ions, lecs)
+    g = GpuSim(cfg)
+    g.set_fields(**f)
+    g.sync_from_host()
+    g.set_particles(ions, lecs)
+    g.step(3)
+    o.step(3)
+    for species in (0, 1):
+        for stride in (1, 3, 10):
+            a, b = g.output_particles(species, stride), o.output_particles(species, stride)
+            assert len(a["ind"]) == len(b["ind"]) > 0
+            ia, ib = np.argsort(a["ind"], kind="stable"), np.argsort(b["ind"], kind="stable")
+            for k in a:
+                np.testing.assert_array_equal(a[k][ia], b[k][ib], err_msg=f"{species} {stride} {k}")
+    g.close()

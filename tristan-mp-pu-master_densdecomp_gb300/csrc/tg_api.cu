@@ -11,6 +11,7 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "tg_internal.cuh"
 #include "tg_spectrum.cuh"
@@ -1723,6 +1724,57 @@ extern "C" int tg_output_var(tg_ctx *ctx, int32_t var, int32_t istep, int32_t id
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
     cudaFree(d_out);
     if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_output_var: %s", cudaGetErrorString(e));
+    return check_status(ctx);
+}
+
+extern "C" int tg_output_particles(tg_ctx *ctx, int32_t species, int32_t stride, int64_t cap, float *vals,
+                                   int32_t *ids, int64_t *count) {
+    if (!ctx || !count || species < 0 || species > 1 || stride < 1 || cap < 0) return TG_ERR_ARG;
+    if (cap > 0 && (!vals || !ids)) return TG_ERR_ARG;
+    long long n[2];
+    int r = exact_counts(ctx, n);
+    if (r) return r;
+    const long long m = n[species];
+    *count = 0;
+    if (m == 0) return TG_OK;
+    if (m > INT32_MAX) return fail(ctx, TG_ERR_ARG, "tg_output_particles: species too large to scan");
+    const Species &sp = ctx->sp[ctx->par][species];
+    int *flag = nullptr, *pos = nullptr;
+    void *tmp = nullptr;
+    size_t tbytes = 0;
+    float *d_vals = nullptr;
+    int *d_ids = nullptr;
+    cudaError_t e = cudaMalloc(&flag, (size_t)m * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&pos, (size_t)m * 4);
+    if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(nullptr, tbytes, flag, pos, (int)m, ctx->st);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, tbytes);
+    if (e == cudaSuccess) e = launch_prt_flag(sp, m, stride, flag, ctx->st);
+    if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(tmp, tbytes, flag, pos, (int)m, ctx->st);
+    int last[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&last[0], pos + m - 1, 4, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&last[1], flag + m - 1, 4, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    const long long total = (long long)last[0] + last[1];
+    if (e == cudaSuccess && total > 0 && total <= cap) {
+        e = cudaMalloc(&d_vals, (size_t)total * 8 * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&d_ids, (size_t)total * 2 * 4);
+        if (e == cudaSuccess) e = launch_prt_write(ctx->g, ctx->P, sp, m, flag, pos, total, d_vals, d_ids, ctx->st);
+        // the device arrays are total long; the caller's are cap long
+        for (int k = 0; k < 8 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(vals + (size_t)k * cap, d_vals + (size_t)k * total, (size_t)total * 4,
+                                cudaMemcpyDeviceToHost, ctx->st);
+        for (int k = 0; k < 2 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(ids + (size_t)k * cap, d_ids + (size_t)k * total, (size_t)total * 4,
+                                cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    }
+    cudaFree(flag);
+    cudaFree(pos);
+    cudaFree(tmp);
+    cudaFree(d_vals);
+    cudaFree(d_ids);
+    if (e != cudaSuccess) return fail(ctx, TG_ERR_CUDA, "tg_output_particles: %s", cudaGetErrorString(e));
+    *count = total;
     return check_status(ctx);
 }
 

@@ -422,6 +422,57 @@ cudaError_t launch_output_sample(const Geom &g, int comp, const float *a, float 
 }
 
 // ---------------------------------------------------------------------------
+// output_tot's particle sample (prtl.tot): particles with
+// modulo(ind / 2, stride) = 0, compacted in the device's order
+// ---------------------------------------------------------------------------
+__global__ void k_prt_flag(Species sp, long long n, int stride, int *flag) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int h = sp.ind[t] / 2;  // Fortran integer division: toward zero
+        flag[t] = (sp.cell[t] >= 0 && ((h % stride) + stride) % stride == 0) ? 1 : 0;
+    }
+}
+
+// vals: x + mxcum, y + mycum, z + mzcum, u, v, w, ch, gamma (cap each);
+// ids: ind, proc (cap each)
+template <int DIM>
+__global__ void k_prt_write(Geom g, Params P, Species sp, long long n, const int *flag, const int *pos,
+                            long long cap, float *vals, int *ids) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        if (!flag[t]) continue;
+        const long long o = pos[t];
+        float x, y, z;
+        load_pos<DIM>(g, sp, t, x, y, z);
+        const float u = sp.u[t], v = sp.v[t], w = sp.w[t];
+        vals[o] = x + (float)P.mxcum;
+        vals[cap + o] = y + (float)P.mycum;
+        vals[2 * cap + o] = z + (float)P.mzcum;
+        vals[3 * cap + o] = u;
+        vals[4 * cap + o] = v;
+        vals[5 * cap + o] = w;
+        vals[6 * cap + o] = sp.ch[t];
+        vals[7 * cap + o] = sqrtf(1.0f + (u * u + v * v + w * w));
+        ids[o] = sp.ind[t];
+        ids[cap + o] = sp.proc[t];
+    }
+}
+
+cudaError_t launch_prt_flag(const Species &sp, long long n, int stride, int *flag, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_prt_flag<<<dgrid(n), 256, 0, st>>>(sp, n, stride, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prt_write(const Geom &g, const Params &P, const Species &sp, long long n, const int *flag,
+                             const int *pos, long long cap, float *vals, int *ids, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (g.dims == 3) k_prt_write<3><<<dgrid(n), 256, 0, st>>>(g, P, sp, n, flag, pos, cap, vals, ids);
+    else k_prt_write<2><<<dgrid(n), 256, 0, st>>>(g, P, sp, n, flag, pos, cap, vals, ids);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // flow-frame energy spectra per slice (save_spectrum_2d,
 // code/output.F90:794-1249)
 // ---------------------------------------------------------------------------

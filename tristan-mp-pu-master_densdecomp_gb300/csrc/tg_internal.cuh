@@ -478,6 +478,11 @@ cudaError_t launch_spec_species(const Geom &g, const Params &P, const SpecGrid &
 // the array itself, at nodes start + istep (a, b, c), a < n[0] ... (tg_diag.cu)
 cudaError_t launch_output_sample(const Geom &g, int comp, const float *a, float add, const int start[3],
                                  const int n[3], int istep, float *out, cudaStream_t st);
+// output_tot's particle sample: flags of the selected particles, and the
+// compacted values at the scanned positions (tg_diag.cu)
+cudaError_t launch_prt_flag(const Species &sp, long long n, int stride, int *flag, cudaStream_t st);
+cudaError_t launch_prt_write(const Geom &g, const Params &P, const Species &sp, long long n, const int *flag,
+                             const int *pos, long long cap, float *vals, int *ids, cudaStream_t st);
 // grid moments (meanq_fld_cur) into f3[0] (moment) and f3[1] (weight);
 // num / den are zeroed FP64 scratch of g.lot cells, left zeroed
 cudaError_t launch_moments(const Geom &g, const Params &P, const Species *sp, const long long *count, long long hint,

@@ -200,6 +200,15 @@ module m_tristan_gpu_3d
        integer(c_int32_t), value :: var, istep, idx, idy, idz
        type(c_ptr), value :: out
      end function
+     integer(c_int) function tg_output_particles(ctx, species, stride, cap, vals, ids, count) &
+         bind(C, name="tg_output_particles")
+       import :: c_int, c_ptr, c_int32_t, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: species, stride
+       integer(c_int64_t), value :: cap
+       type(c_ptr), value :: vals, ids
+       integer(c_int64_t), intent(out) :: count
+     end function
      integer(c_int) function tg_spectrum_x_bins(ctx, nbins) bind(C, name="tg_spectrum_x_bins")
        import :: c_int, c_ptr, c_int32_t
        type(c_ptr), value :: ctx
@@ -232,7 +241,8 @@ module m_tristan_gpu_3d
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
             gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
             gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
-            gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum, gpu_output_var
+            gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum, gpu_output_var, &
+            gpu_output_particles
 
 contains
 
@@ -386,6 +396,19 @@ contains
     real, target, intent(out) :: out(:,:,:)
     call check(tg_output_var(ctx, int(var, c_int32_t), int(istep, c_int32_t), 2_c_int32_t, 2_c_int32_t, &
                merge(0_c_int32_t, 2_c_int32_t, mz == 1), c_loc(out)), "output_tot")
+  end subroutine
+
+  ! output_tot's particle sample of one species (0 ions, 1 electrons): the
+  ! particles with modulo(ind/2, stride) = 0; vals(:, 1:8) = x+mxcum,
+  ! y+mycum, z+mzcum, u, v, w, ch, gamma and ids(:, 1:2) = ind, proc for
+  ! the first count rows (count > size(vals, 1): only count is set)
+  subroutine gpu_output_particles(species, stride, vals, ids, count)
+    integer, intent(in) :: species, stride
+    real, target, intent(out) :: vals(:,:)
+    integer, target, intent(out) :: ids(:,:)
+    integer(c_int64_t), intent(out) :: count
+    call check(tg_output_particles(ctx, int(species, c_int32_t), int(stride, c_int32_t), &
+               int(size(vals, 1), c_int64_t), c_loc(vals), c_loc(ids), count), "output_tot particles")
   end subroutine
 
   ! save_spectrum's arrays from the device (code/output.F90:380-785): nbins

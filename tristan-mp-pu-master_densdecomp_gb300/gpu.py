@@ -122,7 +122,7 @@ ENTRY_POINTS = (
     "tg_ens_get_counts", "tg_ens_synchronize", "tg_ens_kernels_per_step", "tg_ens_autotune",
     "tg_shock_init", "tg_shock_get", "tg_inject_region", "tg_particle_bc", "tg_field_bc", "tg_inject",
     "tg_write_restart", "tg_read_restart", "tg_moments", "tg_spectrum_dims", "tg_spectrum", "tg_spectrum_x_bins",
-    "tg_spectrum_x", "tg_output_dims", "tg_output_var",
+    "tg_spectrum_x", "tg_output_dims", "tg_output_var", "tg_output_particles",
 )
 # grid moments of meanq_fld_cur (code/output.F90:5222-5482), by the reference's names
 MOMENTS = ("tdens", "idens", "tbetx", "tbety", "tbetz", "ibetx", "ibety", "ibetz", "tmomx", "tmomy", "tmomz",
@@ -203,6 +203,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.tg_output_dims.restype = ctypes.c_int
     lib.tg_output_var.argtypes = [P] + [ctypes.c_int32] * 5 + [P]
     lib.tg_output_var.restype = ctypes.c_int
+    lib.tg_output_particles.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, P, P,
+                                        ctypes.POINTER(ctypes.c_int64)]
+    lib.tg_output_particles.restype = ctypes.c_int
     lib.tg_spectrum_x_bins.argtypes = [P, ctypes.POINTER(ctypes.c_int32)]
     lib.tg_spectrum_x_bins.restype = ctypes.c_int
     lib.tg_spectrum_x.argtypes = [P, ctypes.c_int32] + [P] * 7
@@ -565,6 +568,21 @@ class GpuSim:
         out = np.zeros(int(dims.prod()), np.float32)
         self._check(self.lib.tg_output_var(self.h, int(var), istep, idx, idy, idz, out.ctypes.data))
         return out.reshape(dims[2], dims[1], dims[0])
+
+    def output_particles(self, species: int, stride: int) -> dict:
+        """output_tot's particle sample (prtl.tot) of one species: the
+        particles with modulo(ind / 2, stride) = 0, device order"""
+        cnt = ctypes.c_int64()
+        self._check(self.lib.tg_output_particles(self.h, species, stride, 0, None, None, ctypes.byref(cnt)))
+        cap = max(cnt.value, 1)
+        vals = np.zeros((8, cap), np.float32)
+        ids = np.zeros((2, cap), np.int32)
+        self._check(self.lib.tg_output_particles(self.h, species, stride, cap, vals.ctypes.data, ids.ctypes.data,
+                                                 ctypes.byref(cnt)))
+        names = ("x", "y", "z", "u", "v", "w", "ch", "gamma")
+        out = {k: vals[i, :cnt.value] for i, k in enumerate(names)}
+        out["ind"], out["proc"] = ids[0, :cnt.value], ids[1, :cnt.value]
+        return out
 
     def spectrum_x(self, gambins: int = 200) -> dict:
         """lab-frame and flow-frame energy spectra per x slice, divided by
