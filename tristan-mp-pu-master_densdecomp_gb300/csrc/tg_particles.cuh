@@ -128,22 +128,24 @@ __device__ __forceinline__ void block_accumulate(double *vals, double *acc, int 
 // ---------------------------------------------------------------------------
 // Deposit sinks
 // ---------------------------------------------------------------------------
-// Shared-memory deposit window in exact fixed point. A contribution
-// q (|q| < 2^31 units) is split into q = qh*2^16 + ql, ql in [0, 2^16), and
-// the two parts go into two 32-bit accumulators with native, non-returning
-// 32-bit shared atomic adds (FP32 shared atomics are compare-and-swap loops
-// on this GPU: a load, an add, a CAS and a branch per update). Exact for up to
-// 65536 contributions per cell and tile: the low sums stay below 2^32 and the
-// high sums inside int32. Value = hi * 2^16 + lo.
+// Shared-memory deposit window in exact fixed point, two 32-bit words per
+// cell updated with native, non-returning 32-bit shared atomic adds (FP32
+// shared atomics are compare-and-swap loops on this GPU). With
+// q = qh*2^16 + ql, ql in [0, 2^16) (|q| < 2^31 units), lo sums q itself
+// modulo 2^32 and hi sums qh. For up to 65536 contributions per cell and
+// tile the sum L of the ql stays below 2^32, so L = lo - hi*2^16 modulo 2^32
+// and the value is hi*2^16 + L; hi stays inside int32.
 __device__ __forceinline__ void fx_add_shared(unsigned *lo, int *hi, int idx, long long q) {
     const int q32 = (int)q;  // callers guarantee |q| < 2^31
-    atomicAdd(lo + idx, (unsigned)(q32 & 0xffff));
+    atomicAdd(lo + idx, (unsigned)q32);
     const int qh = q32 >> 16;  // arithmetic shift: floor division by 2^16
     if (qh != 0) atomicAdd(hi + idx, qh);
 }
 
 __device__ __forceinline__ long long fx_read_shared(const unsigned *lo, const int *hi, int idx) {
-    return (long long)hi[idx] * 65536LL + (long long)lo[idx];
+    const int h = hi[idx];
+    const unsigned l16 = lo[idx] - ((unsigned)h << 16);
+    return (long long)h * 65536LL + (long long)l16;
 }
 
 template <bool FIXED>
