@@ -138,8 +138,9 @@ __device__ __forceinline__ void block_accumulate(double *vals, double *acc, int 
 __device__ __forceinline__ void fx_add_shared(unsigned *lo, int *hi, int idx, long long q) {
     const int q32 = (int)q;  // callers guarantee |q| < 2^31
     atomicAdd(lo + idx, (unsigned)q32);
-    const int qh = q32 >> 16;  // arithmetic shift: floor division by 2^16
-    if (qh != 0) atomicAdd(hi + idx, qh);
+    // arithmetic shift: floor division by 2^16; added even when zero (a
+    // test and a predicated atomic cost more issue slots than the update)
+    atomicAdd(hi + idx, q32 >> 16);
 }
 
 __device__ __forceinline__ long long fx_read_shared(const unsigned *lo, const int *hi, int idx) {
