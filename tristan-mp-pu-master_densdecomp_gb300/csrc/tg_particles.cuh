@@ -177,7 +177,7 @@ struct WindowSink {
     // otherwise at cell (i, j, k) of the global arrays
     __device__ __forceinline__ void add_at(int comp, int widx, bool in, int i, int j, int k, float v) {
         const float x = v * scale;
-        if (in && fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact split path
+        if (in && fabsf(x) < 1073741824.0f) {  // below 2^30 units: exact window sums
             fx_add_shared(lo, hi, comp * wcells + widx, to_fixed32(x));
             return;
         }
