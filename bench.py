@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-fixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--host-parts", type=int, default=0,
+                    help="parts per species of the end-to-end lap (0: by size)")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--sort-every", type=int, default=0, help="0: chosen by the autotuner")
     ap.add_argument("--no-autotune", action="store_true")
@@ -220,6 +222,7 @@ def run_e2e(cfg, ions, lecs, args, device):
     cfg.fixed = 0
     sim = GpuSim(cfg, device=device, pinned=True)
     sim.set_particles(ions, lecs, upload=False)
+    sim.set_host_parts(args.host_parts)
     up = SYNC_E | SYNC_B | SYNC_PARTICLES
     sim.sync_from_host(SYNC_ALL)
     sim.step_host(1)
@@ -232,6 +235,31 @@ def run_e2e(cfg, ions, lecs, args, device):
     dt = time.perf_counter() - t0
     sim.close()
     return dt, h2d, d2h
+
+
+def copy_only_ms(h2d, d2h, device, reps=3):
+    """the same bytes moved between page-locked host memory and the device
+    with nothing else running, both directions at once (one stream each):
+    the link's bound for one end-to-end step"""
+    import torch
+    dev = torch.device("cuda", device)
+    hu = torch.empty(h2d, dtype=torch.uint8, pin_memory=True)
+    hd = torch.empty(d2h, dtype=torch.uint8, pin_memory=True)
+    du = torch.empty(h2d, dtype=torch.uint8, device=dev)
+    dd = torch.empty(d2h, dtype=torch.uint8, device=dev)
+    s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    for r in range(reps + 1):
+        if r == 1:
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+        with torch.cuda.stream(s_up):
+            du.copy_(hu, non_blocking=True)
+        with torch.cuda.stream(s_down):
+            hd.copy_(dd, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    del hu, hd, du, dd
+    return ms
 
 
 def cpu_baseline(cfg, ions, lecs, steps):
@@ -448,10 +476,17 @@ def main():
         fixed = {"value": ws * n_p * args.steps / (ms_f / 1e3), "ms_per_step": ms_f / args.steps,
                  "particle_kernel_ms": ph_f["particles"], "deposit": "int64 fixed point (bit-reproducible)"}
     dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, args, device)
+    ms_e2e = dt_e2e / args.e2e_steps * 1e3
+    ms_link = copy_only_ms(h2d, d2h, device)
     e2e = {"value": ws * n_p * args.e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h,
+           "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
+           "link": {"bound": "host link (NVLink-C2C), both directions at once",
+                    "copy_only_ms": ms_link, "achieved_gbs": (h2d + d2h) / ms_e2e / 1e6,
+                    "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e},
            "mode": "one tg_step_host call per lap: E, B, particle records up; the lap; fields, "
-                        "records, counts down (one species' transfer overlaps the other's sort and push)"}
+                        "records, counts down (each species in parts: a part is sorted and pushed as soon "
+                        "as it is in, and goes home while later parts arrive)",
+           "host_parts": args.host_parts or "by size"}
     peak, peak_kind = measured_peak_hbm()
     t_kernel = phases["particles"] / 1e3
     alg = tile_kernel_bytes(cfg, n_p, False)

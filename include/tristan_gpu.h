@@ -165,15 +165,26 @@ int tg_step(tg_ctx *ctx, int32_t nsteps);
    keeps its own arrays between laps: per lap E, B and the particle records
    (tg_bind_fields / tg_bind_particles) go to the device, the lap runs, and
    E, B, the currents, the records and the counts come back before the call
-   returns. With page-locked host records on an all-periodic domain the
-   record transfers of one species overlap the other species' sort and push
-   and the field phases; otherwise it is tg_sync_from_host + tg_step(1) +
-   tg_sync_to_host per lap. */
+   returns. With page-locked host records on an all-periodic domain each
+   species travels in parts (tg_set_host_parts): a part is sorted and
+   pushed as soon as its records are in, and sent home while later parts
+   are still arriving; otherwise it is tg_sync_from_host + tg_step(1) +
+   tg_sync_to_host per lap. The records come back in the device's order
+   (each part grouped by tile), not in the order they went up. */
 int tg_step_host(tg_ctx *ctx, int32_t nsteps);
+/* Parts per species for the overlapped tg_step_host, 1..TG_HOST_PARTS_MAX;
+   0 (the default) picks by size: one part per 2^22 records of the larger
+   species, at most TG_HOST_PARTS_MAX. No counterpart in the reference. */
+#define TG_HOST_PARTS_MAX 8
+int tg_set_host_parts(tg_ctx *ctx, int32_t parts);
 /* Page-lock the bound host arrays (the nine fields and 2 * maxhlf particle
    records) so host transfers run as asynchronous DMA; arrays already
-   page-locked are left as they are. Undone by tg_finalize. No counterpart
-   in the reference. */
+   page-locked are left as they are. Before locking a range it asks the
+   kernel for transparent huge pages behind it (madvise MADV_HUGEPAGE, and
+   MADV_COLLAPSE where the kernel has it): locked base pages sustain fewer
+   bytes per second over the host link with both directions in flight.
+   Undone by tg_finalize (the advice stays). No counterpart in the
+   reference. */
 int tg_pin_host(tg_ctx *ctx);
 /* tg_step bracketed by CUDA events on the context's stream; *ms receives
    the device time of the nsteps laps. Synchronises. */

@@ -1,6 +1,8 @@
 // C-ABI of the GB300 TRISTAN-MP hot path: context, device memory, the
 // per-subroutine entry points and the fused, graph-captured lap.
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -79,12 +81,17 @@ struct tg_ctx {
     tg_shock hshock;
     // grid-moment scratch (FP64 sums)
     double *mom[2] = {};
-    // host-driven laps (tg_step_host): copy streams, events, staging copy of
-    // the host records (both species)
+    // host-driven laps (tg_step_host): copy streams, events (one link, then
+    // uploaded / pushed per species and part), staging copy of the host
+    // records (both species), the parts each species travels in
     cudaStream_t st_up = nullptr, st_down = nullptr;
-    cudaEvent_t ev_link[5] = {};
+    cudaEvent_t ev_link[1 + 4 * TG_HOST_PARTS_MAX] = {};
     void *stage2 = nullptr;
     long long host_n[2] = {0, 0};
+    int host_parts = 0;                        // 0: by size
+    int *ptstart[2][TG_HOST_PARTS_MAX] = {};   // tile starts of parts 1.. (part 0: tstart)
+    long long *d_pcnt = nullptr;               // [species][part][records, sorted]
+    long long pcnt[2][TG_HOST_PARTS_MAX][2] = {};
     std::vector<void *> pinned;  // host ranges page-locked by tg_pin_host
     char err[512] = {0};
     std::vector<void *> allocs;
@@ -423,6 +430,41 @@ static int ensure_sorted(tg_ctx *ctx) {
     return sort_all(ctx, false);
 }
 
+// The overlapped host-driven lap (tg_step_host): the records of each species
+// travel by DMA (copy engines, no SMs) between the page-locked host array and
+// a device staging copy of it, in parts of consecutive records; each part is
+// converted and tile-sorted on its own as soon as its records are in, pushed
+// by its own tile launch, converted back and sent home while later parts are
+// still arriving and the field phases run. Part h of species s holds records
+// [off[s][h], off[s][h+1]) in the host array, the staging copy and both
+// particle parities.
+struct HostPipe {
+    char *host;             // the bound host records
+    char *stage;            // device staging copy, same layout
+    cudaStream_t down;      // device -> host copies
+    int parts;
+    long long off[2][TG_HOST_PARTS_MAX + 1];
+    cudaEvent_t uploaded[2][TG_HOST_PARTS_MAX], pushed[2][TG_HOST_PARTS_MAX];
+    const int *ts[2][TG_HOST_PARTS_MAX];  // tile starts per part
+};
+
+// the records [o, ...) of a species as a species of their own
+static Species species_at(const Species &s, long long o) {
+    Species v = s;
+    v.cell += o;
+    v.ox += o;
+    v.oy += o;
+    v.oz += o;
+    v.u += o;
+    v.v += o;
+    v.w += o;
+    v.ch += o;
+    v.ind += o;
+    v.proc += o;
+    v.splitlev += o;
+    return v;
+}
+
 static TileArgs tile_args(tg_ctx *ctx, bool count_tiles) {
     TileArgs a;
     memset(&a, 0, sizeof a);
@@ -740,7 +782,8 @@ extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
 // ---------------------------------------------------------------------------
 // FP64 diagnostics
 // ---------------------------------------------------------------------------
-static int run_diag(tg_ctx *ctx, bool particles) {
+// pipe: the particles are grouped by tile part by part (a host-driven lap)
+static int run_diag(tg_ctx *ctx, bool particles, const HostPipe *pipe = nullptr) {
     DiagLaunch d;
     memset(&d, 0, sizeof d);
     d.g = ctx->g;
@@ -749,6 +792,14 @@ static int run_diag(tg_ctx *ctx, bool particles) {
         d.sp[s] = ctx->sp[ctx->par][s];
         d.tstart[s] = ctx->tstart[s];
         d.mass[s] = fabsf(ctx->P.qs[s] / ctx->P.qm[s]);
+    }
+    if (pipe && pipe->parts > 1) {
+        d.nparts = pipe->parts;
+        for (int h = 0; h < pipe->parts; h++)
+            for (int s = 0; s < 2; s++) {
+                d.psp[h][s] = species_at(ctx->sp[ctx->par][s], pipe->off[s][h]);
+                d.pts[h][s] = pipe->ts[s][h];
+            }
     }
     for (int a = 0; a < 6; a++) d.f[a] = ctx->f[a];
     d.rhofx = ctx->rhofx;
@@ -998,18 +1049,6 @@ static cudaError_t mark(tg_ctx *ctx, int li, int phase, int end) {
     return cudaEventRecord(ctx->ev[((size_t)li * TG_NPHASES + phase) * 2 + end], ctx->st);
 }
 
-// The overlapped host-driven lap (tg_step_host): the records of each species
-// travel by DMA (copy engines, no SMs) between the page-locked host array and
-// a device staging copy of it; each species is converted and sorted as soon
-// as its records are in, pushed by its own tile launch, converted back and
-// sent home while the other species and the field phases run.
-struct HostPipe {
-    char *host;             // the bound host records
-    char *stage;            // device staging copy, same layout
-    cudaStream_t down;      // device -> host copies
-    cudaEvent_t uploaded[2], pushed[2];
-};
-
 static int sort_species(tg_ctx *ctx, int s, bool counted);
 
 static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const HostPipe *pipe = nullptr) {
@@ -1031,31 +1070,50 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
     CK(mark(ctx, li, 0, 1));
     CK(mark(ctx, li, 1, 0));
     if (pipe) {
-        // species by species: the freshly uploaded records into the particle
-        // arrays, the tile sort (into the other parity), the push, and the
-        // records back to the staging copy, from where they go home
+        // part by part: the freshly uploaded records into the particle
+        // arrays, the part's tile sort (into the other parity), its push, and
+        // its records back to the staging copy, from where they go home
         const int p0 = ctx->par;
         CK(cudaMemsetAsync(ctx->d_dead, 0, sizeof(int), st));  // the sorts compact
         ctx->fault_seen = false;
         for (int s = 0; s < 2; s++) {
-            const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
-            CK(cudaStreamWaitEvent(st, pipe->uploaded[s], 0));
-            CK(launch_aos_to_soa(g, pipe->stage + off, ctx->sp[p0][s], ctx->host_n[s], ctx->d_status, st));
-            int rr = sort_species(ctx, s, false);
-            if (rr) return rr;
-            TileArgs a = tile_args(ctx, false);
-            a.sp[s] = ctx->sp[1 - p0][s];  // this species is sorted already
-            a.only = s + 1;
-            CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st));
-            CK(launch_soa_to_aos(g, ctx->sp[1 - p0][s], pipe->stage + off, ctx->host_n[s], st));
-            CK(cudaEventRecord(pipe->pushed[s], st));
-            CK(cudaStreamWaitEvent(pipe->down, pipe->pushed[s], 0));
-            CK(cudaMemcpyAsync(pipe->host + off, pipe->stage + off, (size_t)ctx->host_n[s] * AOS,
-                               cudaMemcpyDeviceToHost, pipe->down));
-            k += 6;
+            const size_t soff = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+            // a record dropped on the way up leaves its part one entry short:
+            // the entries no sort fills read as dropped
+            if (pipe->parts > 1)
+                CK(cudaMemsetAsync(ctx->sp[1 - p0][s].cell, 0xff, (size_t)ctx->host_n[s] * 4, st));
+            for (int h = 0; h < pipe->parts; h++) {
+                const long long o = pipe->off[s][h], m = pipe->off[s][h + 1] - o;
+                const Species src = species_at(ctx->sp[p0][s], o), dst = species_at(ctx->sp[1 - p0][s], o);
+                char *stg = pipe->stage + soff + (size_t)o * AOS;
+                // the part's record count in, its sorted count out
+                long long *cin = ctx->d_cnt + 2 * p0 + s, *cout = ctx->d_cnt + 2 * (1 - p0) + s;
+                if (pipe->parts > 1) {
+                    cin = ctx->d_pcnt + 2 * (s * TG_HOST_PARTS_MAX + h);
+                    cout = cin + 1;
+                }
+                CK(cudaStreamWaitEvent(st, pipe->uploaded[s][h], 0));
+                CK(launch_aos_to_soa(g, stg, src, m, ctx->d_status, st));
+                CK(launch_tile_count(g, src, cin, m, ctx->hist[s], st));
+                int *ts = const_cast<int *>(pipe->ts[s][h]);
+                CK(launch_scan(ctx->hist[s], ts, ctx->cursor[s], g.ntiles, cout, st));
+                CK(launch_scatter(g, src, dst, cin, m, ts, ctx->cursor[s], st));
+                TileArgs a = tile_args(ctx, false);
+                a.sp[s] = dst;
+                a.tstart[s] = ts;
+                a.only = s + 1;
+                CK(launch_tiles(a, ctx->P.fixed != 0, true, true, st));
+                CK(launch_soa_to_aos(g, dst, stg, m, st));
+                CK(cudaEventRecord(pipe->pushed[s][h], st));
+                CK(cudaStreamWaitEvent(pipe->down, pipe->pushed[s][h], 0));
+                CK(cudaMemcpyAsync(pipe->host + soff + (size_t)o * AOS, stg, (size_t)m * AOS,
+                                   cudaMemcpyDeviceToHost, pipe->down));
+                k += 6;
+            }
         }
         ctx->par = 1 - p0;
-        ctx->dirty = false;
+        // in parts the species is grouped by tile part by part only
+        ctx->dirty = pipe->parts > 1;
         ctx->may_have_dead = false;
     }
     TileArgs a = tile_args(ctx, sort_now);
@@ -1108,9 +1166,9 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
     }
     if (ctx->cfg.diag_every > 0) {
         CK(mark(ctx, li, 5, 0));
-        int rr = run_diag(ctx, true);
+        int rr = run_diag(ctx, true, pipe);
         if (rr) return rr;
-        k += 4 + ctx->g.dims * ctx->cfg.ntimes;
+        k += 4 + ctx->g.dims * ctx->cfg.ntimes + (pipe ? pipe->parts - 1 : 0);
         CK(mark(ctx, li, 5, 1));
     }
     *nk = k;
@@ -1230,30 +1288,62 @@ static int host_lap(tg_ctx *ctx) {
     pipe.host = (char *)ctx->hp;
     pipe.stage = (char *)ctx->stage2;
     pipe.down = ctx->st_down;
-    pipe.uploaded[0] = ctx->ev_link[0];
-    pipe.uploaded[1] = ctx->ev_link[1];
-    pipe.pushed[0] = ctx->ev_link[2];
-    pipe.pushed[1] = ctx->ev_link[3];
     cudaStream_t st = ctx->st;
     const size_t lot = (size_t)g.lot;
     CK(cudaStreamSynchronize(st));
+    // parts per species: as set, else one per 2^22 records of the larger species
+    int parts = ctx->host_parts;
+    if (parts == 0) {
+        const long long big = n[0] > n[1] ? n[0] : n[1];
+        parts = (int)(big >> 22);
+        parts = parts < 1 ? 1 : parts > TG_HOST_PARTS_MAX ? TG_HOST_PARTS_MAX : parts;
+    }
+    pipe.parts = parts;
+    if (parts > 1 && !ctx->d_pcnt) {
+        int rr = dalloc(ctx, &ctx->d_pcnt, (size_t)4 * TG_HOST_PARTS_MAX);
+        for (int s = 0; s < 2 && !rr; s++)
+            for (int h = 1; h < TG_HOST_PARTS_MAX && !rr; h++)
+                rr = dalloc(ctx, &ctx->ptstart[s][h], (size_t)g.ntiles + 1);
+        if (rr) return rr;
+    }
+    for (int s = 0; s < 2; s++) {
+        for (int h = 0; h <= parts; h++) {
+            // part boundaries on multiples of 32 records (whole 128-byte lines of the arrays)
+            pipe.off[s][h] = h == parts ? n[s] : (n[s] * h / parts) & ~31LL;
+            if (h < parts) {
+                pipe.ts[s][h] = h == 0 ? ctx->tstart[s] : ctx->ptstart[s][h];
+                pipe.uploaded[s][h] = ctx->ev_link[1 + 2 * (s * TG_HOST_PARTS_MAX + h)];
+                pipe.pushed[s][h] = ctx->ev_link[2 + 2 * (s * TG_HOST_PARTS_MAX + h)];
+            }
+        }
+        for (int h = 0; h < parts; h++) ctx->pcnt[s][h][0] = pipe.off[s][h + 1] - pipe.off[s][h];
+    }
     for (int s = 0; s < 2; s++) {
         ctx->host_n[s] = n[s];
         ctx->hcount[s] = n[s];
         CK(cudaMemcpyAsync(ctx->d_cnt + 2 * ctx->par + s, &ctx->host_n[s], sizeof(long long),
                            cudaMemcpyHostToDevice, st));
+        // in parts the counts of the lap's parity are the whole species'
+        if (parts > 1)
+            CK(cudaMemcpyAsync(ctx->d_cnt + 2 * (1 - ctx->par) + s, &ctx->host_n[s], sizeof(long long),
+                               cudaMemcpyHostToDevice, st));
     }
+    if (parts > 1)
+        CK(cudaMemcpyAsync(ctx->d_pcnt, ctx->pcnt, sizeof ctx->pcnt, cudaMemcpyHostToDevice, st));
     // E and B first: host-to-device copies leave in the order they are
     // issued, and the lap's first phases need the fields only
     for (int a = 0; a < 6; a++) CK(cudaMemcpyAsync(ctx->f[a], ctx->hf[a], lot * 4, cudaMemcpyHostToDevice, st));
     // the records go up by DMA once earlier work on the stream is done
-    CK(cudaEventRecord(ctx->ev_link[4], st));
-    CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_link[4], 0));
+    CK(cudaEventRecord(ctx->ev_link[0], st));
+    CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_link[0], 0));
     for (int s = 0; s < 2; s++) {
-        const size_t off = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
-        CK(cudaMemcpyAsync(pipe.stage + off, pipe.host + off, (size_t)n[s] * AOS, cudaMemcpyHostToDevice,
-                           ctx->st_up));
-        CK(cudaEventRecord(pipe.uploaded[s], ctx->st_up));
+        const size_t soff = s == 0 ? 0 : (size_t)ctx->cfg.maxhlf * AOS;
+        for (int h = 0; h < parts; h++) {
+            const size_t o = soff + (size_t)pipe.off[s][h] * AOS;
+            CK(cudaMemcpyAsync(pipe.stage + o, pipe.host + o, (size_t)(pipe.off[s][h + 1] - pipe.off[s][h]) * AOS,
+                               cudaMemcpyHostToDevice, ctx->st_up));
+            CK(cudaEventRecord(pipe.uploaded[s][h], ctx->st_up));
+        }
     }
     int nk = 0;
     int r = lap_kernels(ctx, false, &nk, 1 << 20, &pipe);
@@ -1263,8 +1353,8 @@ static int host_lap(tg_ctx *ctx) {
     ctx->last_direct = true;
     ctx->lap += 1;
     for (int a = 0; a < 9; a++) CK(cudaMemcpyAsync(ctx->hf[a], ctx->f[a], lot * 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaEventRecord(ctx->ev_link[4], ctx->st_down));
-    CK(cudaStreamWaitEvent(st, ctx->ev_link[4], 0));
+    CK(cudaEventRecord(ctx->ev_link[0], ctx->st_down));
+    CK(cudaStreamWaitEvent(st, ctx->ev_link[0], 0));
     int flags[2] = {0, 0};
     CK(cudaMemcpyAsync(&flags[0], ctx->d_dead, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&flags[1], ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1278,6 +1368,31 @@ static int host_lap(tg_ctx *ctx) {
     *ctx->hions = (int32_t)n[0];
     *ctx->hlecs = (int32_t)n[1];
     return TG_OK;
+}
+
+extern "C" int tg_set_host_parts(tg_ctx *ctx, int32_t parts) {
+    if (!ctx) return TG_ERR_ARG;
+    if (parts < 0 || parts > TG_HOST_PARTS_MAX)
+        return fail(ctx, TG_ERR_ARG, "tg_set_host_parts: parts %d outside [0, %d]", parts, TG_HOST_PARTS_MAX);
+    ctx->host_parts = parts;
+    return TG_OK;
+}
+
+#ifndef MADV_COLLAPSE
+#define MADV_COLLAPSE 25  // Linux 6.1+: back the populated range with huge pages now
+#endif
+// Ask for transparent huge pages behind a host range before it is
+// page-locked: page-locked base pages sustain fewer bytes per second over
+// the host link when both directions are in flight. Advice only: a kernel
+// or mapping that refuses it leaves the range as it was.
+static void advise_huge_pages(void *h, size_t len) {
+    const long ps = sysconf(_SC_PAGESIZE);
+    if (ps <= 0) return;
+    const uintptr_t a = ((uintptr_t)h + (uintptr_t)ps - 1) & ~((uintptr_t)ps - 1);
+    const uintptr_t b = ((uintptr_t)h + len) & ~((uintptr_t)ps - 1);
+    if (b <= a) return;
+    (void)madvise((void *)a, b - a, MADV_HUGEPAGE);
+    (void)madvise((void *)a, b - a, MADV_COLLAPSE);
 }
 
 extern "C" int tg_pin_host(tg_ctx *ctx) {
@@ -1297,6 +1412,7 @@ extern "C" int tg_pin_host(tg_ctx *ctx) {
         cudaPointerAttributes at;
         if (cudaPointerGetAttributes(&at, h[i]) == cudaSuccess && at.type == cudaMemoryTypeHost) continue;
         (void)cudaGetLastError();
+        advise_huge_pages(h[i], len[i]);
         cudaError_t e = cudaHostRegister(h[i], len[i], cudaHostRegisterDefault);
         if (e == cudaErrorHostMemoryAlreadyRegistered) {
             (void)cudaGetLastError();

@@ -642,13 +642,20 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
         if (e != cudaSuccess) return e;                                                                 \
         k_diag_particles<D, O><<<g.ntiles, 256, smem, st>>>(a);                                         \
     } while (0)
-    if (!d.particles) {
-    } else if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
-    else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
-    else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
-    else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);
-    else if (g.dims == 3 && g.order == 2) TG_DL(3, 2);
-    else TG_DL(3, 3);
+    for (int h = 0; h < (d.nparts > 0 ? d.nparts : 1); h++) {
+        if (d.nparts > 0)
+            for (int s = 0; s < 2; s++) {
+                a.sp[s] = d.psp[h][s];
+                a.tstart[s] = d.pts[h][s];
+            }
+        if (!d.particles) {
+        } else if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
+        else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
+        else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
+        else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);
+        else if (g.dims == 3 && g.order == 2) TG_DL(3, 2);
+        else TG_DL(3, 3);
+    }
 #undef TG_DL
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = g.dims == 3 ? g.mz - g.ngz : 1;

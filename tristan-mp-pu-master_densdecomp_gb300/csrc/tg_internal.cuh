@@ -464,6 +464,11 @@ struct DiagLaunch {
     int ntimes;
     int *status;
     bool particles;  // false: the lap's tile kernel already summed the particles
+    // nparts > 0: the particles are grouped by tile part by part (a
+    // host-driven lap); the particle pass runs once per part
+    int nparts;
+    Species psp[TG_HOST_PARTS_MAX][2];
+    const int *pts[TG_HOST_PARTS_MAX][2];
 };
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
 // flow-frame spectra (save_spectrum_2d): the gamma range (two float bit

@@ -147,6 +147,11 @@ module m_tristan_gpu_3d
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
      end function
+     integer(c_int) function tg_set_host_parts(ctx, parts) bind(C, name="tg_set_host_parts")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: parts
+     end function
      ! collisionless-shock hooks (user_pu/user_shock_pu.F90)
      integer(c_int) function tg_shock_init(ctx, k) bind(C, name="tg_shock_init")
        import :: c_int, c_ptr, tg_shock
