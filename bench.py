@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--workload", default="twostream2d_1024_o3")
     ap.add_argument("--no-fixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--host-parts", type=int, default=0,
                     help="parts per species of the end-to-end lap (0: by size)")
     ap.add_argument("--cpu-steps", type=int, default=3)

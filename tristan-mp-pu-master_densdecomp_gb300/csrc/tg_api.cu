@@ -1157,6 +1157,14 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
         k += 4;
     }
     CK(mark(ctx, li, 3, 1));
+    if (pipe) {
+        // the fields are final here (the diagnostics only read them): they
+        // go home while the diagnostics run
+        CK(cudaEventRecord(ctx->ev_link[0], st));
+        CK(cudaStreamWaitEvent(pipe->down, ctx->ev_link[0], 0));
+        for (int f9 = 0; f9 < 9; f9++)
+            CK(cudaMemcpyAsync(ctx->hf[f9], ctx->f[f9], (size_t)g.lot * 4, cudaMemcpyDeviceToHost, pipe->down));
+    }
     if (sort_now && !pipe) {
         CK(mark(ctx, li, 4, 0));
         int rr = sort_all(ctx, true);
@@ -1306,10 +1314,19 @@ static int host_lap(tg_ctx *ctx) {
                 rr = dalloc(ctx, &ctx->ptstart[s][h], (size_t)g.ntiles + 1);
         if (rr) return rr;
     }
+    // the first part of the first species and the last part of the second
+    // get a third of the others' share: only one direction of the link is
+    // busy while the first part goes up and while the last one comes home
+    long long cum[2][TG_HOST_PARTS_MAX + 1];
+    for (int s = 0; s < 2; s++) {
+        cum[s][0] = 0;
+        for (int h = 0; h < parts; h++)
+            cum[s][h + 1] = cum[s][h] + ((parts > 1 && h == (s == 0 ? 0 : parts - 1)) ? 1 : 3);
+    }
     for (int s = 0; s < 2; s++) {
         for (int h = 0; h <= parts; h++) {
             // part boundaries on multiples of 32 records (whole 128-byte lines of the arrays)
-            pipe.off[s][h] = h == parts ? n[s] : (n[s] * h / parts) & ~31LL;
+            pipe.off[s][h] = h == parts ? n[s] : (n[s] * cum[s][h] / cum[s][parts]) & ~31LL;
             if (h < parts) {
                 pipe.ts[s][h] = h == 0 ? ctx->tstart[s] : ctx->ptstart[s][h];
                 pipe.uploaded[s][h] = ctx->ev_link[1 + 2 * (s * TG_HOST_PARTS_MAX + h)];
@@ -1352,7 +1369,6 @@ static int host_lap(tg_ctx *ctx) {
     ctx->last_laps = 1;
     ctx->last_direct = true;
     ctx->lap += 1;
-    for (int a = 0; a < 9; a++) CK(cudaMemcpyAsync(ctx->hf[a], ctx->f[a], lot * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ctx->ev_link[0], ctx->st_down));
     CK(cudaStreamWaitEvent(st, ctx->ev_link[0], 0));
     int flags[2] = {0, 0};
