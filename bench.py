@@ -15,8 +15,9 @@ Arms:
                     beside it, the dominant kernel's roofline, the CPU
                     baseline, the end-to-end figure and the SM clocks.
   --impl reference  the reference algorithm on the host cores: the OpenMP
-                    build of the CPU restatement (no Fortran compiler exists
-                    on the box, so the reference itself cannot be built).
+                    build of the CPU restatement (the reference is Fortran
+                    with MPI, and no Fortran compiler is installed, so the
+                    reference itself cannot be built).
 
 Multi-GPU: the path does not shard (one domain, no collectives); N ranks
 run N independent replicas and `value` sums them (weak scaling).
@@ -510,7 +511,7 @@ def main():
         dt_cpu, cores = cpu_baseline(cfg, ions, lecs, args.cpu_steps)
         cpu = {"value": n_p * args.cpu_steps / dt_cpu, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_steps} full laps of the workload (after 1 warm-up lap) on the OpenMP "
-                         "CPU restatement; the Fortran reference cannot be built on the box"}
+                         "CPU restatement; the Fortran reference cannot be built (no Fortran compiler)"}
     ens = None
     if rank == 0 and not args.no_ensemble:
         ens = run_ensemble(args, device)

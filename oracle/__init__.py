@@ -1,6 +1,6 @@
 """CPU oracle for the TRISTAN-MP hot path (test infrastructure only).
 
-This package is the checker used by ``tests/``, ``__graft_entry__.smoke()``
+This package is the oracle used by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline leg of ``bench.py``. The GPU product path never imports
 it. It wraps ``tristan_oracle.c`` (a restatement of the reference Fortran in
 the reference's floating-point operation order) through ctypes.

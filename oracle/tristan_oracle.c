@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the TRISTAN-MP per-step PIC hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker): the tests, the smoke check and
+ * TEST INFRASTRUCTURE ONLY (the oracle): the tests, the smoke check and
  * bench.py's CPU-baseline leg call it; the GPU product path never does.
  *
  * Each function restates one reference subroutine in the reference's own

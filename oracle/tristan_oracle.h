@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the TRISTAN-MP per-step PIC hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker: the tests, the
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle: the tests, the
  * smoke check and the CPU-baseline leg of bench.py call it to produce the
  * reference answer. The GPU product path never links, loads or calls it.
  *
