@@ -1,8 +1,9 @@
 """Physics known-answer tests that pin the oracle where the reference ships
 no golden vectors: B-spline partition of unity, per-particle discrete charge
 continuity of the Esirkepov current, Gauss's law under the binomial filter
-over a Weibel run, the Yee vacuum dispersion relation with Corr, and the
-plasma frequency of the reference's charge normalisation."""
+over a Weibel run, the Yee vacuum dispersion relation with Corr, the
+plasma frequency of the reference's charge normalisation and the linear
+growth rate of the two-stream instability."""
 import math
 
 import numpy as np
@@ -153,6 +154,47 @@ def test_plasma_oscillation_frequency(order, lo, hi):
     assert len(t) >= 5
     w = math.pi / float(np.mean(np.diff(t)))
     assert lo < w / wp < hi, w / wp
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_two_stream_growth_rate(order):
+    """Two cold pair beams at +-0.5c (the two-stream workload's plasma, here
+    cold) in a box 4 cells high, so the electrostatic mode along x is the
+    only fast one: the box's longest mode grows at the rate of the cold
+    relativistic two-beam dispersion relation
+    1 = a [1/(w - k v0)^2 + 1/(w + k v0)^2], a = w_p^2 / (2 g0^3),
+    w_p^2 = (c/c_omp)^2 g0 with the reference's normalisation of the
+    charge (code/particles.F90:189-256; longitudinal mass g0^3 m). The rate
+    is fitted to ln|E_x(k)| over the linear phase; order 2 sits lowest (its
+    truncated gather, as for the plasma frequency)."""
+    nx, ny = 64, 4
+    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=0.5, delgam=0.0,
+                    ntimes=0)
+    ions, lecs = setups.load_beams(cfg, seed=5)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    x0 = cfg.nghost // 2 + 1
+    kk = 2 * math.pi / nx
+    lecs["u"] = (lecs["u"] + 1e-4 * np.sin(kk * (lecs["x"] - x0))).astype(np.float32)
+    sim = oracle.OracleSim(cfg)
+    sim.set_particles(ions, lecs)
+    xe = (np.arange(cfg.mx) + 1) + 0.5 - x0
+    si, sj = slice(x0 - 1, x0 - 1 + nx), slice(x0 - 1, x0 - 1 + ny)
+    bs, bc = np.sin(kk * xe[si]), np.cos(kk * xe[si])
+    amp = []
+    for _ in range(650):
+        sim.step()
+        ex = sim.field("ex")[0, sj, si].mean(axis=0)
+        amp.append(math.hypot(float(ex @ bs), float(ex @ bc)))
+    amp = np.array(amp)
+    assert amp[649] > 100 * amp[299]  # still growing, not saturated
+    rate = np.polyfit(np.arange(300, 650), np.log(amp[300:650]), 1)[0]
+    g0 = cfg.gamma_drift
+    kv = kk * cfg.c * math.sqrt(1.0 - 1.0 / g0 ** 2)
+    a = (cfg.c / cfg.c_omp) ** 2 * g0 / (2.0 * g0 ** 3)
+    # (w^2 - kv^2)^2 = 2a (w^2 + kv^2), a quadratic in w^2
+    w2 = np.roots([1.0, -(2.0 * kv ** 2 + 2.0 * a), kv ** 4 - 2.0 * a * kv ** 2])
+    theory = float(np.sqrt(w2.astype(complex)).imag.max())
+    assert 0.95 < rate / theory < 1.03, (rate, theory)
 
 
 def test_x_slice_spectrum_weights_and_axes():
