@@ -3,7 +3,7 @@ no golden vectors: B-spline partition of unity, per-particle discrete charge
 continuity of the Esirkepov current, Gauss's law under the binomial filter
 over a Weibel run, the Yee vacuum dispersion relation with Corr, the
 plasma frequency of the reference's charge normalisation and the linear
-growth rate of the two-stream instability."""
+growth rates of the two-stream and Weibel (filamentation) instabilities."""
 import math
 
 import numpy as np
@@ -195,6 +195,49 @@ def test_two_stream_growth_rate(order):
     w2 = np.roots([1.0, -(2.0 * kv ** 2 + 2.0 * a), kv ** 4 - 2.0 * a * kv ** 2])
     theory = float(np.sqrt(w2.astype(complex)).imag.max())
     assert 0.95 < rate / theory < 1.03, (rate, theory)
+
+
+@pytest.mark.parametrize("order,mode", [(1, 2), (2, 3), (3, 1), (3, 2), (3, 3)])
+def test_weibel_growth_rate(order, mode):
+    """Cold pair beams at gamma0 = 3 streaming along +-x (the Weibel
+    workload's plasma, here cold) in a box 4 cells long and 64 high: a
+    filamentation mode k along y, seeded by a small net electron current,
+    grows at the rate of the cold relativistic filamentation dispersion
+    relation w^2 - k^2 c^2 - w_p^2 / g0^3 - w_p^2 b0^2 k^2 c^2 / (g0 w^2) = 0
+    (E along the beams, longitudinal mass g0^3 m, transverse g0 m;
+    w_p^2 = (c/c_omp)^2 g0 from the reference's charge normalisation). The
+    rate is fitted to ln|B_z(k)| over the linear phase."""
+    nx, ny = 4, 64
+    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=3.0, delgam=0.0,
+                    ntimes=0)
+    ions, lecs = setups.load_beams(cfg, seed=9)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    x0 = cfg.nghost // 2 + 1
+    kk = 2 * math.pi * mode / ny
+    # ions and electrons of a cold pair move together (no current): the
+    # seed speeds up one beam's electrons where the other's slow down
+    lecs["u"] = (lecs["u"] + 1e-4 * np.abs(lecs["u"]) * np.sin(kk * (lecs["y"] - x0))).astype(np.float32)
+    sim = oracle.OracleSim(cfg)
+    sim.set_particles(ions, lecs)
+    ye = (np.arange(cfg.my) + 1) + 0.5 - x0
+    si, sj = slice(x0 - 1, x0 - 1 + nx), slice(x0 - 1, x0 - 1 + ny)
+    bs, bc = np.sin(kk * ye[sj]), np.cos(kk * ye[sj])
+    amp = []
+    for _ in range(250):
+        sim.step()
+        bz = sim.field("bz")[0, sj, si].mean(axis=1)
+        amp.append(math.hypot(float(bz @ bs), float(bz @ bc)))
+    amp = np.array(amp)
+    assert amp[249] > 100 * amp[100]
+    rate = np.polyfit(np.arange(100, 250), np.log(amp[100:250]), 1)[0]
+    g0 = cfg.gamma_drift
+    b0 = math.sqrt(1.0 - 1.0 / g0 ** 2)
+    c = cfg.c
+    wp2 = (c / cfg.c_omp) ** 2 * g0
+    bq = kk ** 2 * c ** 2 + wp2 / g0 ** 3
+    cq = wp2 * b0 ** 2 * kk ** 2 * c ** 2 / g0
+    theory = math.sqrt((math.sqrt(bq * bq + 4.0 * cq) - bq) / 2.0)
+    assert 0.95 < rate / theory < 1.05, (rate, theory)
 
 
 def test_x_slice_spectrum_weights_and_axes():
