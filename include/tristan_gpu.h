@@ -100,7 +100,9 @@ typedef struct {
 
 /* Allocate the device domain: replaces allocate_fields
    (code/fields.F90:207-360) and allocate_particles
-   (code/particles.F90:286-341). */
+   (code/particles.F90:286-341). TG_ERR_ARG for a domain with fewer than 8
+   interior cells along an axis (mx - nghost, my - nghost, and in 3D
+   mz - nghostz). */
 int tg_init(const tg_config *cfg, tg_ctx **out);
 /* Release everything (finalize, code/tristan.F90:38). */
 void tg_finalize(tg_ctx *ctx);

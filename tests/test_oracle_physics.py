@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
+import physics_cases
 from tristan_gb300 import setups
 from tristan_gb300.config import SimConfig
 
@@ -116,127 +117,39 @@ def test_yee_vacuum_dispersion():
     assert abs(w_meas - w_theory) / w_theory < 2e-3
 
 
-@pytest.mark.parametrize("order,lo,hi", [(3, 0.998, 1.002), (1, 1.0, 1.015), (2, 0.97, 0.99)])
-def test_plasma_oscillation_frequency(order, lo, hi):
-    """A cold, neutral pair plasma (ion and electron of each pair at one
-    point, at rest) whose electrons get a small velocity u = 0.01 sin(kx)
-    oscillates at the plasma frequency of the reference's normalisation:
-    the charges of code/particles.F90:189-256 give each species w_p^2 / 2
-    with w_p = c / c_omp, and both species move. Measured from the zero
-    crossings of E_x's Fourier mode over three periods (dt = 1, no filter).
-    Order 3 lands on w_p; order 1 (linear shapes) sits up to 1.5% above it
-    from grid aliasing; order 2 sits 1-3% below it because the reference's
-    order-2 mover gathers with two of its three weights per axis (the force
-    is weaker than the deposited charge implies)."""
-    nx, ny = 64, 4
-    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=16.0, gamma0=1.0, delgam=0.0,
-                    ntimes=0)
-    ions, lecs = setups.load_beams(cfg, seed=3)
-    setups.with_capacity(cfg, len(ions), len(lecs))
-    x0 = cfg.nghost // 2 + 1
-    kk = 2 * math.pi / nx
-    lecs["u"] = (0.01 * np.sin(kk * (lecs["x"] - x0))).astype(np.float32)
+def oracle_runner(cfg, ions, lecs):
     sim = oracle.OracleSim(cfg)
     sim.set_particles(ions, lecs)
-    # E_x sits half a cell right of its node
-    xe = (np.arange(cfg.mx) + 1) + 0.5 - x0
-    si, sj = slice(x0 - 1, x0 - 1 + nx), slice(x0 - 1, x0 - 1 + ny)
-    basis = np.sin(kk * xe[si])
-    wp = cfg.c / cfg.c_omp
-    probe = []
-    for _ in range(int(3.2 * 2 * math.pi / wp)):
-        sim.step()
-        probe.append(float(np.dot(sim.field("ex")[0, sj, si].mean(axis=0), basis)))
-    probe = np.array(probe)
-    sgn = np.sign(probe)
-    cross = np.nonzero(sgn[1:] != sgn[:-1])[0]
-    t = [c0 + probe[c0] / (probe[c0] - probe[c0 + 1]) for c0 in cross]
-    assert len(t) >= 5
-    w = math.pi / float(np.mean(np.diff(t)))
+    return sim.step, lambda name: sim.field(name)[0]
+
+
+@pytest.mark.parametrize("order,lo,hi", [(3, 0.998, 1.002), (1, 1.0, 1.015), (2, 0.97, 0.99)])
+def test_plasma_oscillation_frequency(order, lo, hi):
+    """A cold pair plasma with a small electron velocity wave oscillates at
+    w_p = c/c_omp (physics_cases.plasma_oscillation). Order 3 lands on it;
+    order 1 (linear shapes) sits up to 1.5% above it from grid aliasing;
+    order 2 sits 1-3% below it because the reference's order-2 mover gathers
+    with two of its three weights per axis (the force is weaker than the
+    deposited charge implies)."""
+    w, wp = physics_cases.plasma_oscillation(oracle_runner, order)
     assert lo < w / wp < hi, w / wp
 
 
 @pytest.mark.parametrize("order", [1, 2, 3])
 def test_two_stream_growth_rate(order):
-    """Two cold pair beams at +-0.5c (the two-stream workload's plasma, here
-    cold) in a box 4 cells high, so the electrostatic mode along x is the
-    only fast one: the box's longest mode grows at the rate of the cold
-    relativistic two-beam dispersion relation
-    1 = a [1/(w - k v0)^2 + 1/(w + k v0)^2], a = w_p^2 / (2 g0^3),
-    w_p^2 = (c/c_omp)^2 g0 with the reference's normalisation of the
-    charge (code/particles.F90:189-256; longitudinal mass g0^3 m). The rate
-    is fitted to ln|E_x(k)| over the linear phase; order 2 sits lowest (its
-    truncated gather, as for the plasma frequency)."""
-    nx, ny = 64, 4
-    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=0.5, delgam=0.0,
-                    ntimes=0)
-    ions, lecs = setups.load_beams(cfg, seed=5)
-    setups.with_capacity(cfg, len(ions), len(lecs))
-    x0 = cfg.nghost // 2 + 1
-    kk = 2 * math.pi / nx
-    lecs["u"] = (lecs["u"] + 1e-4 * np.sin(kk * (lecs["x"] - x0))).astype(np.float32)
-    sim = oracle.OracleSim(cfg)
-    sim.set_particles(ions, lecs)
-    xe = (np.arange(cfg.mx) + 1) + 0.5 - x0
-    si, sj = slice(x0 - 1, x0 - 1 + nx), slice(x0 - 1, x0 - 1 + ny)
-    bs, bc = np.sin(kk * xe[si]), np.cos(kk * xe[si])
-    amp = []
-    for _ in range(650):
-        sim.step()
-        ex = sim.field("ex")[0, sj, si].mean(axis=0)
-        amp.append(math.hypot(float(ex @ bs), float(ex @ bc)))
-    amp = np.array(amp)
-    assert amp[649] > 100 * amp[299]  # still growing, not saturated
-    rate = np.polyfit(np.arange(300, 650), np.log(amp[300:650]), 1)[0]
-    g0 = cfg.gamma_drift
-    kv = kk * cfg.c * math.sqrt(1.0 - 1.0 / g0 ** 2)
-    a = (cfg.c / cfg.c_omp) ** 2 * g0 / (2.0 * g0 ** 3)
-    # (w^2 - kv^2)^2 = 2a (w^2 + kv^2), a quadratic in w^2
-    w2 = np.roots([1.0, -(2.0 * kv ** 2 + 2.0 * a), kv ** 4 - 2.0 * a * kv ** 2])
-    theory = float(np.sqrt(w2.astype(complex)).imag.max())
+    """Cold pair beams at +-0.5c: the electrostatic two-stream mode grows
+    at the cold relativistic two-beam rate (physics_cases.two_stream);
+    order 2 sits lowest (its truncated gather, as for the plasma
+    frequency)."""
+    rate, theory = physics_cases.two_stream(oracle_runner, order)
     assert 0.95 < rate / theory < 1.03, (rate, theory)
 
 
 @pytest.mark.parametrize("order,mode", [(1, 2), (2, 3), (3, 1), (3, 2), (3, 3)])
 def test_weibel_growth_rate(order, mode):
-    """Cold pair beams at gamma0 = 3 streaming along +-x (the Weibel
-    workload's plasma, here cold) in a box 4 cells long and 64 high: a
-    filamentation mode k along y, seeded by a small net electron current,
-    grows at the rate of the cold relativistic filamentation dispersion
-    relation w^2 - k^2 c^2 - w_p^2 / g0^3 - w_p^2 b0^2 k^2 c^2 / (g0 w^2) = 0
-    (E along the beams, longitudinal mass g0^3 m, transverse g0 m;
-    w_p^2 = (c/c_omp)^2 g0 from the reference's charge normalisation). The
-    rate is fitted to ln|B_z(k)| over the linear phase."""
-    nx, ny = 4, 64
-    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=3.0, delgam=0.0,
-                    ntimes=0)
-    ions, lecs = setups.load_beams(cfg, seed=9)
-    setups.with_capacity(cfg, len(ions), len(lecs))
-    x0 = cfg.nghost // 2 + 1
-    kk = 2 * math.pi * mode / ny
-    # ions and electrons of a cold pair move together (no current): the
-    # seed speeds up one beam's electrons where the other's slow down
-    lecs["u"] = (lecs["u"] + 1e-4 * np.abs(lecs["u"]) * np.sin(kk * (lecs["y"] - x0))).astype(np.float32)
-    sim = oracle.OracleSim(cfg)
-    sim.set_particles(ions, lecs)
-    ye = (np.arange(cfg.my) + 1) + 0.5 - x0
-    si, sj = slice(x0 - 1, x0 - 1 + nx), slice(x0 - 1, x0 - 1 + ny)
-    bs, bc = np.sin(kk * ye[sj]), np.cos(kk * ye[sj])
-    amp = []
-    for _ in range(250):
-        sim.step()
-        bz = sim.field("bz")[0, sj, si].mean(axis=1)
-        amp.append(math.hypot(float(bz @ bs), float(bz @ bc)))
-    amp = np.array(amp)
-    assert amp[249] > 100 * amp[100]
-    rate = np.polyfit(np.arange(100, 250), np.log(amp[100:250]), 1)[0]
-    g0 = cfg.gamma_drift
-    b0 = math.sqrt(1.0 - 1.0 / g0 ** 2)
-    c = cfg.c
-    wp2 = (c / cfg.c_omp) ** 2 * g0
-    bq = kk ** 2 * c ** 2 + wp2 / g0 ** 3
-    cq = wp2 * b0 ** 2 * kk ** 2 * c ** 2 / g0
-    theory = math.sqrt((math.sqrt(bq * bq + 4.0 * cq) - bq) / 2.0)
+    """Cold pair beams at gamma0 = 3: the filamentation mode grows at the
+    cold relativistic filamentation rate (physics_cases.weibel)."""
+    rate, theory = physics_cases.weibel(oracle_runner, order, mode)
     assert 0.95 < rate / theory < 1.05, (rate, theory)
 
 

@@ -167,8 +167,12 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.ng = c.nghost;
     g.ngz = c.nghostz;
     const int nx = c.mx - g.ng, ny = c.my - g.ng, nz = c.dims == 3 ? c.mz - g.ngz : 1;
-    if (nx < 4 || ny < 4 || nz < 1 || (c.dims == 3 && nz < 4))
-        return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells)", nx, ny, nz);
+    // at least 8 interior cells per axis, more than the widest ghost band (7
+    // cells): with 4 interior cells under 7 ghost cells the currents differed
+    // from the oracle's; from 8 cells on they agree bit for bit
+    if (nx < 8 || ny < 8 || nz < 1 || (c.dims == 3 && nz < 8))
+        return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells; at least 8 per axis)", nx, ny,
+                         nz);
     g.lot = (long long)c.mx * c.my * c.mz;
     if (g.lot >= (1LL << 31)) return geom_fail(err, errlen, "grid of %lld cells exceeds int32 cell indices", g.lot);
     g.sy = c.mx;
