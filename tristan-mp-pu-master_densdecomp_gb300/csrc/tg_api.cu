@@ -167,9 +167,10 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.ng = c.nghost;
     g.ngz = c.nghostz;
     const int nx = c.mx - g.ng, ny = c.my - g.ng, nz = c.dims == 3 ? c.mz - g.ngz : 1;
-    // at least 8 interior cells per axis, more than the widest ghost band (7
-    // cells): with 4 interior cells under 7 ghost cells the currents differed
-    // from the oracle's; from 8 cells on they agree bit for bit
+    // at least 8 interior cells per axis, no fewer than the widest ghost band
+    // (7 cells): the current fold adds both ghost slabs of an axis in one
+    // launch, and with fewer interior cells than ghost cells the two slabs'
+    // target layers overlap (the reference folds one slab after the other)
     if (nx < 8 || ny < 8 || nz < 1 || (c.dims == 3 && nz < 8))
         return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells; at least 8 per axis)", nx, ny,
                          nz);
