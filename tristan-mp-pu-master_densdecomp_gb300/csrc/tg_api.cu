@@ -450,7 +450,7 @@ struct HostPipe {
     int parts;
     long long off[2][TG_HOST_PARTS_MAX + 1];
     cudaEvent_t uploaded[2][TG_HOST_PARTS_MAX], pushed[2][TG_HOST_PARTS_MAX];
-    const int *ts[2][TG_HOST_PARTS_MAX];  // tile starts per part
+    int *ts[2][TG_HOST_PARTS_MAX];  // tile starts per part (written by the part's scan)
 };
 
 // the records [o, ...) of a species as a species of their own
@@ -1100,7 +1100,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
                 CK(cudaStreamWaitEvent(st, pipe->uploaded[s][h], 0));
                 CK(launch_aos_to_soa(g, stg, src, m, ctx->d_status, st));
                 CK(launch_tile_count(g, src, cin, m, ctx->hist[s], st));
-                int *ts = const_cast<int *>(pipe->ts[s][h]);
+                int *ts = pipe->ts[s][h];
                 CK(launch_scan(ctx->hist[s], ts, ctx->cursor[s], g.ntiles, cout, st));
                 CK(launch_scatter(g, src, dst, cin, m, ts, ctx->cursor[s], st));
                 TileArgs a = tile_args(ctx, false);
