@@ -3,8 +3,8 @@ tests: each builds its plasma, runs it through a runner and returns the
 measured rate together with the theory's.
 
 A runner is made by ``make(cfg, ions, lecs)`` and returns ``(step, field)``:
-``step()`` advances one lap, ``field(name)`` returns the (my, mx) plane of a
-field after the lap (z-plane 0)."""
+``step()`` advances one lap, ``field(name)`` returns the field's (mz, my,
+mx) array after the lap."""
 import math
 
 import numpy as np
@@ -22,15 +22,29 @@ def _zero_crossing_rate(probe: np.ndarray) -> float:
     return math.pi / float(np.mean(np.diff(t)))
 
 
-def plasma_oscillation(make, order: int):
+def _plane(a: np.ndarray, cfg) -> np.ndarray:
+    """the (my, mx) plane of a field: 2D z-plane 0, 3D the mean over the
+    interior z-planes"""
+    if cfg.dims == 2:
+        return a[0]
+    z0 = cfg.nghostz // 2 + 1
+    return a[z0 - 1: z0 - 1 + cfg.nz].mean(axis=0)
+
+
+def plasma_oscillation(make, order: int, dims: int = 2):
     """Cold neutral pair plasma (ion and electron of each pair at one point,
     at rest); the electrons get u = 0.01 sin(kx). Returns (measured w,
     w_p = c/c_omp) from the zero crossings of E_x's Fourier mode over three
     periods (dt = 1, no filter). The charges of code/particles.F90:189-256
-    give each species w_p^2 / 2 and both species move."""
+    give each species w_p^2 / 2 and both species move. 2D: box 64 x 8, 8 per
+    cell per species; 3D: box 64 x 8 x 8, 2 per cell per species."""
     nx, ny = 64, 8
-    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=16.0, gamma0=1.0, delgam=0.0,
-                    ntimes=0)
+    if dims == 2:
+        cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=16.0, gamma0=1.0,
+                        delgam=0.0, ntimes=0)
+    else:
+        cfg = SimConfig(dims=3, order=order, nx=nx, ny=ny, nz=8, c=0.45, c_omp=10.0, ppc0=4.0, gamma0=1.0,
+                        delgam=0.0, ntimes=0)
     ions, lecs = setups.load_beams(cfg, seed=3)
     setups.with_capacity(cfg, len(ions), len(lecs))
     x0 = cfg.nghost // 2 + 1
@@ -45,7 +59,7 @@ def plasma_oscillation(make, order: int):
     probe = []
     for _ in range(int(3.2 * 2 * math.pi / wp)):
         step()
-        probe.append(float(np.dot(field("ex")[sj, si].mean(axis=0), basis)))
+        probe.append(float(np.dot(_plane(field("ex"), cfg)[sj, si].mean(axis=0), basis)))
     return _zero_crossing_rate(np.array(probe)), wp
 
 
@@ -70,7 +84,7 @@ def two_stream(make, order: int):
     amp = []
     for _ in range(650):
         step()
-        ex = field("ex")[sj, si].mean(axis=0)
+        ex = _plane(field("ex"), cfg)[sj, si].mean(axis=0)
         amp.append(math.hypot(float(ex @ bs), float(ex @ bc)))
     amp = np.array(amp)
     assert amp[649] > 100 * amp[299]  # still growing, not saturated
@@ -106,7 +120,7 @@ def weibel(make, order: int, mode: int):
     amp = []
     for _ in range(250):
         step()
-        bz = field("bz")[sj, si].mean(axis=1)
+        bz = _plane(field("bz"), cfg)[sj, si].mean(axis=1)
         amp.append(math.hypot(float(bz @ bs), float(bz @ bc)))
     amp = np.array(amp)
     assert amp[249] > 100 * amp[100]

@@ -19,7 +19,7 @@ def gpu_runner(cfg, ions, lecs):
         g.step(1)
         g.sync_to_host(SYNC_E | SYNC_B)
 
-    return step, lambda name: g.field(name)[0]
+    return step, g.field
 
 
 @pytest.fixture(autouse=True)

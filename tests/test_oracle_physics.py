@@ -120,7 +120,7 @@ def test_yee_vacuum_dispersion():
 def oracle_runner(cfg, ions, lecs):
     sim = oracle.OracleSim(cfg)
     sim.set_particles(ions, lecs)
-    return sim.step, lambda name: sim.field(name)[0]
+    return sim.step, sim.field
 
 
 @pytest.mark.parametrize("order,lo,hi", [(3, 0.998, 1.002), (1, 1.0, 1.015), (2, 0.97, 0.99)])
@@ -132,6 +132,15 @@ def test_plasma_oscillation_frequency(order, lo, hi):
     with two of its three weights per axis (the force is weaker than the
     deposited charge implies)."""
     w, wp = physics_cases.plasma_oscillation(oracle_runner, order)
+    assert lo < w / wp < hi, w / wp
+
+
+@pytest.mark.parametrize("order,lo,hi", [(3, 0.998, 1.002), (1, 1.0, 1.015), (2, 0.92, 0.96)])
+def test_plasma_oscillation_frequency_3d(order, lo, hi):
+    """The same plasma in 3D (64 x 8 x 8): order 3 on w_p, order 1 slightly
+    above it, order 2 lower than in 2D (the truncated gather loses a weight
+    along each of three axes)."""
+    w, wp = physics_cases.plasma_oscillation(oracle_runner, order, dims=3)
     assert lo < w / wp < hi, w / wp
 
 
