@@ -56,6 +56,12 @@ module m_tristan_gpu_3d
      integer(c_int32_t) :: totalpartnum
   end type tg_shock
 
+  ! FP64 diagnostics (tg_diag of tristan_gpu.h)
+  type, bind(C) :: tg_diag
+     real(c_double) :: gauss_residual, gauss_abs, rho_norm, e_field, e_mag, e_kin_ions, e_kin_lecs
+     real(c_double) :: p_part(3), p_field(3), charge_total
+  end type tg_diag
+
   interface
      integer(c_int) function tg_init(cfg, ctx) bind(C, name="tg_init")
        import :: tg_config, c_int, c_ptr
@@ -226,6 +232,39 @@ module m_tristan_gpu_3d
        integer(c_int32_t), value :: gambins
        type(c_ptr), value :: si, se, sir, ser, xgamma, xslice, grange
      end function
+     integer(c_int) function tg_spectrum_dims(ctx, gambins, nxbins, nybins) bind(C, name="tg_spectrum_dims")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: gambins
+       integer(c_int32_t), intent(out) :: nxbins, nybins
+     end function
+     integer(c_int) function tg_spectrum(ctx, gambins, si, se, xgamma, xslice, yslice, grange) &
+         bind(C, name="tg_spectrum")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: gambins
+       type(c_ptr), value :: si, se, xgamma, xslice, yslice, grange
+     end function
+     integer(c_int) function tg_output_dims(ctx, istep, dims) bind(C, name="tg_output_dims")
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: istep
+       integer(c_int32_t), intent(out) :: dims(3)
+     end function
+     integer(c_int) function tg_diag_fp64(ctx, out) bind(C, name="tg_diag_fp64")
+       import :: c_int, c_ptr, tg_diag
+       type(c_ptr), value :: ctx
+       type(tg_diag), intent(out) :: out
+     end function
+     integer(c_int) function tg_get_counts(ctx, ions, lecs) bind(C, name="tg_get_counts")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), intent(out) :: ions, lecs
+     end function
+     integer(c_int) function tg_synchronize(ctx) bind(C, name="tg_synchronize")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function
   end interface
 
   type, bind(C) :: tg_restart_meta
@@ -241,13 +280,14 @@ module m_tristan_gpu_3d
   type(c_ptr), save :: ctx = c_null_ptr
   integer(c_int), parameter :: SYNC_E = 1, SYNC_B = 2, SYNC_CUR = 4, SYNC_PARTICLES = 8, SYNC_ALL = 15
 
-  public :: tg_start, tg_stop, tg_download, tg_upload, tg_pin, &
+  public :: tg_start, tg_stop, tg_download, tg_upload, tg_pin, tg_parts, &
             gpu_bc_b1, gpu_bc_e1, gpu_advance_Bhalfstep, gpu_advance_Efield, gpu_move_particles, &
             gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
             gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
             gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
             gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum, gpu_output_var, &
-            gpu_output_particles
+            gpu_output_particles, tg_diag, gpu_diagnostics, gpu_counts, gpu_synchronize, gpu_output_dims, &
+            gpu_spectrum2d_bins, gpu_spectrum2d
 
 contains
 
@@ -312,6 +352,12 @@ contains
   subroutine tg_pin()
     call check(tg_pin_host(ctx), "tg_pin_host")
   end subroutine tg_pin
+
+  ! parts per species of gpu_step_host's transfers (0: by size)
+  subroutine tg_parts(parts)
+    integer, intent(in) :: parts
+    call check(tg_set_host_parts(ctx, int(parts, c_int32_t)), "tg_set_host_parts")
+  end subroutine tg_parts
 
   ! before Diagnostics / output / restart / host-side user hooks
   subroutine tg_download()
@@ -435,6 +481,58 @@ contains
                c_loc(specerest), c_loc(xgamma), c_loc(xslice), c_loc(gr)), "save_spectrum")
     gmin = gr(1)
     gmax = gr(2)
+  end subroutine
+
+  ! save_spectrum_2d (code/output.F90:794-1249): the slice counts for
+  ! gambins bins, then the flow-frame spectra of both species,
+  ! spec(nxbins, nybins, gambins), with the gamma and slice axes
+  subroutine gpu_spectrum2d_bins(gambins, nxbins, nybins)
+    integer, intent(in) :: gambins
+    integer, intent(out) :: nxbins, nybins
+    integer(c_int32_t) :: nx, ny
+    call check(tg_spectrum_dims(ctx, int(gambins, c_int32_t), nx, ny), "save_spectrum_2d")
+    nxbins = int(nx)
+    nybins = int(ny)
+  end subroutine
+
+  subroutine gpu_spectrum2d(gambins, specp, spece, xgamma, xslice, yslice, gmin, gmax)
+    integer, intent(in) :: gambins
+    real, target, intent(out) :: specp(:,:,:), spece(:,:,:), xgamma(:), xslice(:), yslice(:)
+    real, intent(out) :: gmin, gmax
+    real, target :: gr(2)
+    call check(tg_spectrum(ctx, int(gambins, c_int32_t), c_loc(specp), c_loc(spece), c_loc(xgamma), &
+               c_loc(xslice), c_loc(yslice), c_loc(gr)), "save_spectrum_2d")
+    gmin = gr(1)
+    gmax = gr(2)
+  end subroutine
+
+  ! output_tot's sampled grid (mx1, my1, mz1) for the stride istep
+  subroutine gpu_output_dims(istep, dims)
+    integer, intent(in) :: istep
+    integer, intent(out) :: dims(3)
+    integer(c_int32_t) :: d(3)
+    call check(tg_output_dims(ctx, int(istep, c_int32_t), d), "output_tot")
+    dims = int(d)
+  end subroutine
+
+  ! FP64 Gauss residual, field and kinetic energies, momenta of the state
+  subroutine gpu_diagnostics(d)
+    type(tg_diag), intent(out) :: d
+    call check(tg_diag_fp64(ctx, d), "tg_diag_fp64")
+  end subroutine
+
+  ! the particle counts on the device
+  subroutine gpu_counts(nions, nlecs)
+    integer, intent(out) :: nions, nlecs
+    integer(c_int64_t) :: a, b
+    call check(tg_get_counts(ctx, a, b), "tg_get_counts")
+    nions = int(a)
+    nlecs = int(b)
+  end subroutine
+
+  ! wait for the device (reports a device fault as an error)
+  subroutine gpu_synchronize()
+    call check(tg_synchronize(ctx), "tg_synchronize")
   end subroutine
 
   ! the whole periodic lap fused on the device (replaces lines 115-303)
