@@ -97,17 +97,21 @@ def two_stream(make, order: int):
     return rate, float(np.sqrt(w2.astype(complex)).imag.max())
 
 
-def weibel(make, order: int, mode: int):
-    """Cold pair beams at gamma0 = 3 along +-x in a box 8 x 64; the
-    filamentation mode k = 2 pi mode / 64 along y is seeded by a small net
-    electron current (ions and electrons of a cold pair move together, so
-    one beam's electrons speed up where the other's slow down). Returns
-    (fitted growth rate of |B_z(k)| over the linear phase, the cold
-    relativistic filamentation rate: w^2 - k^2 c^2 - w_p^2 / g0^3 -
-    w_p^2 b0^2 k^2 c^2 / (g0 w^2) = 0, E along the beams)."""
+def weibel(make, order: int, mode: int, dims: int = 2):
+    """Cold pair beams at gamma0 = 3 along +-x in a box 8 x 64 (3D: 8 x 64
+    x 8, 2 per cell per species); the filamentation mode k = 2 pi mode / 64
+    along y is seeded by a small net electron current (ions and electrons
+    of a cold pair move together, so one beam's electrons speed up where
+    the other's slow down). Returns (fitted growth rate of |B_z(k)| over the
+    linear phase, the cold relativistic filamentation rate: w^2 - k^2 c^2 -
+    w_p^2 / g0^3 - w_p^2 b0^2 k^2 c^2 / (g0 w^2) = 0, E along the beams)."""
     nx, ny = 8, 64
-    cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=3.0, delgam=0.0,
-                    ntimes=0)
+    if dims == 2:
+        cfg = SimConfig(dims=2, order=order, nx=nx, ny=ny, c=0.45, c_omp=10.0, ppc0=32.0, gamma0=3.0,
+                        delgam=0.0, ntimes=0)
+    else:
+        cfg = SimConfig(dims=3, order=order, nx=nx, ny=ny, nz=8, c=0.45, c_omp=10.0, ppc0=4.0, gamma0=3.0,
+                        delgam=0.0, ntimes=0)
     ions, lecs = setups.load_beams(cfg, seed=9)
     setups.with_capacity(cfg, len(ions), len(lecs))
     x0 = cfg.nghost // 2 + 1

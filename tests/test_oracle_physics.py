@@ -162,6 +162,15 @@ def test_weibel_growth_rate(order, mode):
     assert 0.95 < rate / theory < 1.05, (rate, theory)
 
 
+@pytest.mark.parametrize("order,lo,hi", [(3, 0.95, 1.05), (2, 0.90, 0.97)])
+def test_weibel_growth_rate_3d(order, lo, hi):
+    """The filamentation mode in 3D (8 x 64 x 8): order 3 on the cold rate;
+    order 2 about 6% below it, its truncated gather weakening the force on
+    three axes (as for the 3D plasma frequency)."""
+    rate, theory = physics_cases.weibel(oracle_runner, order, 2, dims=3)
+    assert lo < rate / theory < hi, (rate, theory)
+
+
 def test_x_slice_spectrum_weights_and_axes():
     """save_spectrum's restatement: the slices tile [3, mx0 - 2], the
     lab-frame spectrum times gamma - 1 holds the splitratio^(1 - splitlev)
