@@ -1,19 +1,27 @@
 """Benchmark: particle-steps/s of the TRISTAN-MP hot path on one GB300.
 
-Workload (default): the 2D two-stream/Weibel box of 1024 x 1024 cells,
-3rd-order shapes, 16 particles per cell per species (33.5 M particles),
-4 filter passes, FP64 Gauss-law / energy / momentum diagnostics every lap.
-A "step" is one full lap of the main loop: field advance, push, Esirkepov
-deposit, periodic wrap, current fold, filter, add_current, tile sort and
-the diagnostics. Inputs are seeded synthetic plasmas with the reference
-setup's shapes (tristan_gb300.setups); the particle arrays (~2 GB) are far
-larger than the 129 MB L2, so no flush is needed between laps.
+Workload (default `value`): the 2D two-stream/Weibel box of 1024 x 1024
+cells, 3rd-order shapes, 16 particles per cell per species (33.5 M
+particles), 4 filter passes, FP64 Gauss-law / energy / momentum diagnostics
+every lap. A "step" is one full lap of the main loop: field advance, push,
+Esirkepov deposit, periodic wrap, current fold, filter, add_current, tile
+sort and the diagnostics. Inputs are seeded synthetic plasmas with the
+reference setup's shapes (tristan_gb300.setups); the particle arrays (~2 GB)
+are far larger than the 129 MB L2, so no flush is needed between laps.
+
+The same line carries, with the same fields, `c3`: the 3D Weibel box of
+256^3 cells at order 2 (134 M particles), the configuration the 3D targets
+are stated on; `ensemble`: 64 seeded 2D boxes, batched fixed point against
+the plain form; and `shock`: the 2D pair shock on 8192 x 512 cells.
 
 Arms:
   default           the GB300 C-ABI library; prints one JSON line with the
-                    FP32-atomic form as `value`, the int64 fixed-point form
-                    beside it, the dominant kernel's roofline, the CPU
-                    baseline, the end-to-end figure and the SM clocks.
+                    FP32 deposit form as `value` (each tile's exact
+                    fixed-point sums rounded once to FP32 and added with
+                    FP32 global atomics), the int64 fixed-point form beside
+                    it, the dominant kernel's roofline, the CPU baseline,
+                    the end-to-end figure, the Gauss-law residuals and the
+                    SM clocks.
   --impl reference  the reference algorithm on the host cores: the OpenMP
                     build of the CPU restatement (the reference is Fortran
                     with MPI, and no Fortran compiler is installed, so the
@@ -41,6 +49,8 @@ import __graft_entry__  # noqa: E402
 
 METRIC = "particle-steps/s (push+deposit+fields), batched/fixed-pt vs plain, same GB300"
 UNIT = "particle-steps/s"
+DEFAULT_WORKLOAD = "twostream2d_1024_o3"
+C3_WORKLOAD = "weibel3d_256_o2"
 
 
 def parse():
@@ -49,7 +59,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="twostream2d_1024_o3")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-c3", action="store_true", help="leave out the 3D order-2 record of the default line")
     ap.add_argument("--no-fixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -194,36 +205,44 @@ def tile_kernel_bytes(cfg, n_particles, fixed):
     return 60.0 * n_particles + (24.0 + (24.0 if fixed else 12.0)) * cfg.ncells
 
 
-def run_form(pkg, cfg, ions, lecs, args, fixed, device, ws, local, clocks=False):
+# the two deposit forms, as they are: both sum a tile's FP32 Esirkepov
+# contributions exactly in a fixed-point shared-memory window
+DEPOSIT_FP32 = ("fp32: exact fixed-point tile window, each tile sum rounded once to FP32 and added with "
+                "FP32 global atomics")
+DEPOSIT_FIXED = "int64 fixed point (bit-reproducible)"
+
+
+def run_form(cfg, ions, lecs, warmup, steps, fixed, device, ws, local, clocks=False):
     from tristan_gb300.gpu import GpuSim
     cfg.fixed = int(fixed)
     sim = GpuSim(cfg, device=device)
     sim.set_particles(ions, lecs)
-    sim.step(max(args.warmup, 3))
+    w = max(warmup, 3)
+    sim.step(w)
     sim.synchronize()
     sim.enable_timing(True)
     barrier(ws, local)
     sim.synchronize()
     if clocks:
         with ClockSampler(device) as cs:
-            ms = sim.step_timed(args.steps)
+            ms = sim.step_timed(steps)
         clk = cs.summary()
     else:
-        ms = sim.step_timed(args.steps)
+        ms = sim.step_timed(steps)
         clk = None
     phases = sim.phase_times()
     kps = sim.kernels_per_step()
-    hist = sim.diag_history(1)
+    hist = sim.diag_history(min(w + steps, 1024))
     sim.close()
     return ms, phases, kps, clk, hist
 
 
-def run_e2e(cfg, ions, lecs, args, device):
+def run_e2e(cfg, ions, lecs, e2e_steps, host_parts, device):
     from tristan_gb300.gpu import GpuSim, SYNC_ALL, SYNC_B, SYNC_E, SYNC_PARTICLES
     cfg.fixed = 0
     sim = GpuSim(cfg, device=device, pinned=True)
     sim.set_particles(ions, lecs, upload=False)
-    sim.set_host_parts(args.host_parts)
+    sim.set_host_parts(host_parts)
     up = SYNC_E | SYNC_B | SYNC_PARTICLES
     sim.sync_from_host(SYNC_ALL)
     sim.step_host(1)
@@ -231,7 +250,7 @@ def run_e2e(cfg, ions, lecs, args, device):
     # one tg_step_host call per lap: E, B and the records up, the lap,
     # everything back, as the reference's main loop would drive it
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         sim.step_host(1)
     dt = time.perf_counter() - t0
     sim.close()
@@ -264,24 +283,140 @@ def copy_only_ms(h2d, d2h, device, reps=3):
 
 
 def cpu_baseline(cfg, ions, lecs, steps):
+    """the OpenMP CPU restatement on the host cores: one warm-up lap, then
+    `steps` timed laps; the oracle's FP64 diagnostics after the warm-up lap
+    and after the last lap (outside the timed region)"""
     import oracle
     oracle.build()
     cfg.fixed = 0
     sim = oracle.OracleSim(cfg, openmp=True)
     sim.set_particles(ions, lecs)
     sim.step(1)
+    d_first = sim.diagnostics()
     t0 = time.perf_counter()
     sim.step(steps)
     dt = time.perf_counter() - t0
-    return dt, sim.lib.to_num_threads()
+    d_last = sim.diagnostics()
+    return dt, sim.lib.to_num_threads(), d_first, d_last
+
+
+def species_density_norm(cfg, nions, nlecs):
+    """|rho_s|_2 of one species' mean charge density over the interior
+    cells (unit particle weights, as the loaders make them)"""
+    ncell = cfg.interior_cells
+    return (abs(cfg.qi) * nions + abs(cfg.qe) * nlecs) / (2.0 * ncell) * (ncell ** 0.5)
+
+
+def hist_residual(hist, lap):
+    """(relative, absolute) Gauss residual of 1-based `lap` from a diag
+    history whose first record is lap 1"""
+    if lap < 1 or lap > len(hist) or hist[lap - 1][1] <= 0:
+        return None, None
+    r2, p2 = hist[lap - 1][0], hist[lap - 1][1]
+    return float(np.sqrt(r2 / p2)), float(np.sqrt(r2))
+
+
+def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_steps, sort_every, autotune):
+    """One single-domain workload: the FP32 form timed by CUDA events with
+    the SM clocks sampled (value), the fixed-point form, the end-to-end lap
+    through tg_step_host, the fused kernel's roofline, the CPU baseline and
+    the Gauss-law residuals. Returns the fields of a bench line."""
+    from tristan_gb300 import setups
+    device = local
+    cfg = setups.make_config(name, diag_every=1, sort_every=max(sort_every, 1))
+    ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    n_p = len(ions) + len(lecs)
+    tuned = None
+    if autotune:
+        # tile shape and re-sort cadence for this plasma (before any timing)
+        from tristan_gb300.gpu import autotune as tune
+        best, table = tune(cfg, ions, lecs, laps=2, device=local)
+        tuned = {"tile": list(cfg.tile), "sort_every": cfg.sort_every, "best_ms_per_lap": best,
+                 "candidates": int(len(table))}
+    grid = [cfg.nx, cfg.ny] + ([cfg.nz] if cfg.dims == 3 else [])
+    config = {"workload": name, "grid": grid, "order": cfg.order, "particles": n_p,
+              "ppc_per_species": int(cfg.ppc0 // 2), "ntimes": cfg.ntimes, "deposit": DEPOSIT_FP32,
+              "diagnostics": "fp64 gauss/energy/momentum every lap", "sort_every": cfg.sort_every,
+              "tile": list(cfg.tile), "autotuned": tuned,
+              "l2": "inputs larger than L2 (particle arrays %.1f GB), no flush" % (n_p * 44 / 1e9)}
+    ms, phases, kps, clk, hist = run_form(cfg, ions, lecs, warmup, steps, False, device, ws, local, clocks=True)
+    ms = allreduce_max(ms, ws, args.impl)
+    value = ws * n_p * steps / (ms / 1e3)
+    ms_f, ph_f, _, _, _ = run_form(cfg, ions, lecs, warmup, steps, True, device, ws, local)
+    ms_f = allreduce_max(ms_f, ws, args.impl)
+    fixed = {"value": ws * n_p * steps / (ms_f / 1e3), "ms_per_step": ms_f / steps,
+             "particle_kernel_ms": ph_f["particles"], "deposit": DEPOSIT_FIXED}
+    dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
+    ms_e2e = dt_e2e / e2e_steps * 1e3
+    ms_link = copy_only_ms(h2d, d2h, device)
+    e2e = {"value": ws * n_p * e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
+           "link": {"bound": "host link (NVLink-C2C), both directions at once",
+                    "copy_only_ms": ms_link, "achieved_gbs": (h2d + d2h) / ms_e2e / 1e6,
+                    "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e},
+           "mode": "one tg_step_host call per lap: E, B, particle records up; the lap; fields, "
+                   "records, counts down (each species in parts: a part is sorted and pushed as soon "
+                   "as it is in, and goes home while later parts arrive)",
+           "host_parts": args.host_parts or "by size"}
+    peak, peak_kind = measured_peak_hbm()
+    t_kernel = phases["particles"] / 1e3
+    alg = tile_kernel_bytes(cfg, n_p, False)
+    achieved = alg / t_kernel / 1e9 if t_kernel > 0 else None
+    roofline = {"kernel": "k_tiles<%d,%d> (fused push + Esirkepov deposit + wrap)" % (cfg.dims, cfg.order),
+                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                "traffic": committed_traffic(name, "fp32"),
+                "algorithmic_bytes_per_launch": alg, "launch_ms": phases["particles"]}
+    # the bound the kernel actually sits at: instruction issue (one warp
+    # instruction per clock per SM sub-partition, 4 per SM, at the SM clock
+    # sampled during the timed laps)
+    ninst = committed_instructions(name, "fp32")
+    if ninst and t_kernel > 0 and clk and clk.get("sm_mhz"):
+        issue_peak = 152 * 4 * clk["sm_mhz"] * 1e6
+        roofline["issue"] = {"achieved": ninst / t_kernel, "peak": issue_peak, "unit": "warp-instructions/s",
+                             "frac": ninst / t_kernel / issue_peak, "instructions_per_launch": ninst,
+                             "peak_basis": "152 SMs x 4 issue slots x median SM clock under load"}
+    total_laps = max(warmup, 3) + steps
+    last = min(total_laps, len(hist))
+    r_last, a_last = hist_residual(hist, last)
+    norm_s = species_density_norm(cfg, len(ions), len(lecs))
+    gauss = {"definition": "|div E - F^ntimes(rho)|_2 / |F^ntimes(rho)|_2 over the interior, FP64 on the "
+                           "device; vs_species_density: the same numerator over one species' mean charge "
+                           "density",
+             "lap": last, "residual": r_last,
+             "residual_vs_species_density": (a_last / norm_s) if a_last is not None else None}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu and cpu_steps > 0:
+        dt_cpu, cores, d1, dN = cpu_baseline(cfg, ions, lecs, cpu_steps)
+        cpu = {"value": n_p * cpu_steps / dt_cpu, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cpu_steps} full laps of the workload (after 1 warm-up lap) on the OpenMP "
+                         "CPU restatement; the Fortran reference cannot be built (no Fortran compiler)"}
+        # the reference arithmetic's own residual on the same plasma: the
+        # oracle's FP32 laps against the device's at the same lap
+        g1, _ = hist_residual(hist, 1)
+        gN, _ = hist_residual(hist, 1 + cpu_steps)
+        gauss["reference_arithmetic"] = {
+            "laps": [1, 1 + cpu_steps], "oracle": [d1["gauss_residual"], dN["gauss_residual"]],
+            "gpu": [g1, gN],
+            "note": "the same residual in the CPU restatement of the reference's FP32 arithmetic: the "
+                    "floor is the rounding of each Esirkepov contribution and carry, not the GPU path"}
+    d = hist[-1] if len(hist) else None
+    return {"value": value, "ms_per_step": ms / steps, "config": config, "fixed_point": fixed,
+            "phase_ms_per_lap": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": kps * steps, "gauss": gauss,
+            "gauss_residual_last_lap": (float(np.sqrt(d[0] / d[1])) if d is not None and d[1] > 0 else None)}
 
 
 def run_ensemble(args, device):
     """The 64-box ensemble: the batched fixed-point form (one launch per
     phase for all boxes, graph-replayed) against the plain form (one
-    single-domain context per box, stepped box after box), both on the same
-    seeded boxes, tile shape and sort cadence; no diagnostics in the timed
-    laps of either. Particle-steps/s are aggregated over all boxes."""
+    single-domain context per box, all resident, each lap stepped box after
+    box through tg_step and timed by the host clock around the whole loop,
+    so the host gaps between boxes count), both on the same seeded boxes,
+    tile shape and sort cadence; no diagnostics in the timed laps of either.
+    Particle-steps/s are aggregated over all boxes. The CPU baseline runs
+    the OpenMP restatement box after box (one timed lap each) and sums."""
     from tristan_gb300 import setups
     from tristan_gb300.gpu import EnsembleSim, GpuSim, ensemble_autotune
     t0 = time.perf_counter()
@@ -320,46 +455,90 @@ def run_ensemble(args, device):
         e.step(warm)
         e.synchronize()
         ms = e.step_timed(K)
-        res = max(e.diagnostics(b)["gauss_residual"] for b in range(e.nbox))
+        res, res_s = 0.0, 0.0
+        for b in range(e.nbox):
+            d = e.diagnostics(b)
+            res = max(res, d["gauss_residual"])
+            res_s = max(res_s, d["gauss_abs"] / species_density_norm(cfgs[b], len(parts[b][0]), len(parts[b][1])))
         kps = e.kernels_per_step()
         e.close()
-        return ms, res, kps
+        return ms, res, res_s, kps
 
     if args.workload == "ensemble64" and args.no_fixed:
         # profiling: the batched fixed-point form alone
-        ms_bf, res_bf, kps = batched(True)
+        ms_bf, _, _, kps = batched(True)
         return {"batched_fixed": {"value": n_p * K / (ms_bf / 1e3), "ms_per_step": ms_bf / K}}
 
     def plain(fixed):
-        total = 0.0
-        for b, c in enumerate(cfgs):
-            c.fixed = int(fixed)
-            g = GpuSim(c, device=device)
-            g.set_particles(*parts[b])
-            g.step(warm)
-            g.synchronize()
-            total += g.step_timed(K)
-            g.close()
-        return total
+        """(host wall-clock ms of K laps of every box, the sum of each box's
+        own device time for K laps)"""
+        sims = []
+        try:
+            for b, c in enumerate(cfgs):
+                c.fixed = int(fixed)
+                g = GpuSim(c, device=device)
+                g.set_particles(*parts[b])
+                g.step(warm)
+                sims.append(g)
+            for g in sims:
+                g.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(K):
+                for g in sims:
+                    g.step(1)
+            for g in sims:
+                g.synchronize()
+            wall = (time.perf_counter() - t0) * 1e3
+            dev = sum(g.step_timed(K) for g in sims)
+        finally:
+            for g in sims:
+                g.close()
+        return wall, dev
 
-    ms_bf, res_bf, kps = batched(True)
-    ms_b32, res_b32, _ = batched(False)
-    ms_pf = plain(True)
-    ms_p32 = plain(False)
+    ms_bf, res_bf, res_bf_s, kps = batched(True)
+    ms_b32, res_b32, res_b32_s, _ = batched(False)
+    wall_pf, dev_pf = plain(True)
+    wall_p32, dev_p32 = plain(False)
     rate = lambda ms: n_p * K / (ms / 1e3)
     orders = {o: sum(1 for c in cfgs if c.order == o) for o in (1, 2, 3)}
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        t_cpu, threads = 0.0, 1
+        for b, c in enumerate(cfgs):
+            c.fixed = 0
+            sim = oracle.OracleSim(c, openmp=True)
+            sim.set_particles(*parts[b])
+            sim.step(1)
+            t1 = time.perf_counter()
+            sim.step(1)
+            t_cpu += time.perf_counter() - t1
+            threads = sim.lib.to_num_threads()
+            del sim
+        cpu = {"value": n_p / t_cpu, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "one lap of every box (after one warm-up lap each) on the OpenMP CPU restatement, "
+                         "box after box, summed"}
     return {
         "workload": "ensemble of %d periodic 2D boxes (seeded sides, plasmas, shape orders)" % len(cfgs),
         "boxes": len(cfgs), "particles": n_p, "cells": int(sum(c.nx * c.ny for c in cfgs)),
         "boxes_per_order": orders, "seed": 20240607, "steps": K, "warmup": warm,
         "tile": list(cfgs[0].tile), "sort_every": se, "autotuned": tuned,
-        "batched_fixed": {"value": rate(ms_bf), "ms_per_step": ms_bf / K, "gauss_residual_max": res_bf},
-        "batched_fp32": {"value": rate(ms_b32), "ms_per_step": ms_b32 / K, "gauss_residual_max": res_b32},
-        "plain_fp32": {"value": rate(ms_p32), "ms_per_step": ms_p32 / K,
-                       "form": "one single-domain context per box, boxes stepped one after another"},
-        "plain_fixed": {"value": rate(ms_pf), "ms_per_step": ms_pf / K},
-        "batched_fixed_over_plain_fp32": ms_p32 / ms_bf,
-        "batched_fixed_over_plain_fixed": ms_pf / ms_bf,
+        "batched_fixed": {"value": rate(ms_bf), "ms_per_step": ms_bf / K, "gauss_residual_max": res_bf,
+                          "gauss_residual_vs_species_density_max": res_bf_s},
+        "batched_fp32": {"value": rate(ms_b32), "ms_per_step": ms_b32 / K, "gauss_residual_max": res_b32,
+                         "gauss_residual_vs_species_density_max": res_b32_s},
+        "plain_fp32": {"value": rate(wall_p32), "ms_per_step": wall_p32 / K,
+                       "device_only": {"value": rate(dev_p32), "ms_per_step": dev_p32 / K},
+                       "form": "one single-domain context per box, all resident; each lap every box's tg_step "
+                               "in turn, host wall-clock around the loop (device_only: the boxes' own device "
+                               "times summed, no host gaps)"},
+        "plain_fixed": {"value": rate(wall_pf), "ms_per_step": wall_pf / K,
+                        "device_only": {"value": rate(dev_pf), "ms_per_step": dev_pf / K}},
+        "batched_fixed_over_plain_fp32": wall_p32 / ms_bf,
+        "batched_fixed_over_plain_fixed": wall_pf / ms_bf,
+        "batched_fixed_over_plain_fixed_device_only": dev_pf / ms_bf,
+        "cpu_baseline": cpu,
         "kernels_per_step": kps, "host_load_s": t_load,
     }
 
@@ -402,14 +581,14 @@ def run_shock(args, device):
             "value": mean_n * K / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / K,
             "particles_initial_load": n_load, "particles_timed": [n0, n1],
             "device_load_s": t_load, "xinject2": st["xinject2"], "walloc": st["walloc"],
-            "kernels_per_step": kps, "deposit": "fp32-atomic", "sort_every": se,
+            "kernels_per_step": kps, "deposit": DEPOSIT_FP32, "sort_every": se,
             "hooks": "reflecting wall + zigzag, conductor, moving injector (jump-ahead Park-Miller)"}
 
 
 def main():
     args = parse()
     ws, rank, local = dist_setup(args)
-    pkg = __graft_entry__.load_package()
+    __graft_entry__.load_package()
     if args.workload == "shock2d_8192x512_o3":
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": args.workload,
@@ -422,30 +601,23 @@ def main():
             print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "ensemble64", "ensemble": ens}),
                   flush=True)
         return
-    from tristan_gb300 import setups
-    cfg = setups.make_config(args.workload, diag_every=1, sort_every=max(args.sort_every, 1))
-    ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
-    setups.with_capacity(cfg, len(ions), len(lecs))
-    n_p = len(ions) + len(lecs)
-    tuned = None
-    if args.impl == "gb300" and not args.no_autotune and args.sort_every == 0:
-        # tile shape and re-sort cadence for this plasma (before any timing)
-        from tristan_gb300.gpu import autotune
-        best, table = autotune(cfg, ions, lecs, laps=2, device=local)
-        tuned = {"tile": list(cfg.tile), "sort_every": cfg.sort_every, "best_ms_per_lap": best,
-                 "candidates": int(len(table))}
-    grid = [cfg.nx, cfg.ny] + ([cfg.nz] if cfg.dims == 3 else [])
-    config = {"workload": args.workload, "grid": grid, "order": cfg.order, "particles": n_p,
-              "ppc_per_species": int(cfg.ppc0 // 2), "ntimes": cfg.ntimes, "deposit": "fp32-atomic",
-              "diagnostics": "fp64 gauss/energy/momentum every lap", "sort_every": cfg.sort_every,
-              "tile": list(cfg.tile), "autotuned": tuned,
-              "l2": "inputs larger than L2 (particle arrays %.1f GB), no flush" % (n_p * 44 / 1e9)}
 
     if args.impl == "reference":
         if rank != 0:
             return
+        from tristan_gb300 import setups
         import oracle
         oracle.build()
+        cfg = setups.make_config(args.workload, diag_every=1, sort_every=max(args.sort_every, 1))
+        ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
+        setups.with_capacity(cfg, len(ions), len(lecs))
+        n_p = len(ions) + len(lecs)
+        grid = [cfg.nx, cfg.ny] + ([cfg.nz] if cfg.dims == 3 else [])
+        config = {"workload": args.workload, "grid": grid, "order": cfg.order, "particles": n_p,
+                  "ppc_per_species": int(cfg.ppc0 // 2), "ntimes": cfg.ntimes, "deposit": DEPOSIT_FP32,
+                  "diagnostics": "fp64 gauss/energy/momentum every lap", "sort_every": cfg.sort_every,
+                  "tile": list(cfg.tile), "autotuned": None,
+                  "l2": "inputs larger than L2 (particle arrays %.1f GB), no flush" % (n_p * 44 / 1e9)}
         cfg.fixed = 0
         sim = oracle.OracleSim(cfg, openmp=True)
         sim.set_particles(ions, lecs)
@@ -466,68 +638,33 @@ def main():
         print(json.dumps(line), flush=True)
         return
 
-    device = local
-    ms, phases, kps, clk, hist = run_form(pkg, cfg, ions, lecs, args, False, device, ws, local, clocks=True)
-    ms = allreduce_max(ms, ws, args.impl)
-    value = ws * n_p * args.steps / (ms / 1e3)
-    fixed = None
-    if not args.no_fixed:
-        ms_f, ph_f, _, _, _ = run_form(pkg, cfg, ions, lecs, args, True, device, ws, local)
-        ms_f = allreduce_max(ms_f, ws, args.impl)
-        fixed = {"value": ws * n_p * args.steps / (ms_f / 1e3), "ms_per_step": ms_f / args.steps,
-                 "particle_kernel_ms": ph_f["particles"], "deposit": "int64 fixed point (bit-reproducible)"}
-    dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, args, device)
-    ms_e2e = dt_e2e / args.e2e_steps * 1e3
-    ms_link = copy_only_ms(h2d, d2h, device)
-    e2e = {"value": ws * n_p * args.e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
-           "link": {"bound": "host link (NVLink-C2C), both directions at once",
-                    "copy_only_ms": ms_link, "achieved_gbs": (h2d + d2h) / ms_e2e / 1e6,
-                    "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e},
-           "mode": "one tg_step_host call per lap: E, B, particle records up; the lap; fields, "
-                        "records, counts down (each species in parts: a part is sorted and pushed as soon "
-                        "as it is in, and goes home while later parts arrive)",
-           "host_parts": args.host_parts or "by size"}
-    peak, peak_kind = measured_peak_hbm()
-    t_kernel = phases["particles"] / 1e3
-    alg = tile_kernel_bytes(cfg, n_p, False)
-    achieved = alg / t_kernel / 1e9 if t_kernel > 0 else None
-    roofline = {"kernel": "k_tiles (fused push + Esirkepov deposit + wrap)", "bound": "hbm",
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
-                "traffic": committed_traffic(args.workload, "fp32"),
-                "algorithmic_bytes_per_launch": alg, "launch_ms": phases["particles"]}
-    # the bound the kernel actually sits at: instruction issue (one warp
-    # instruction per clock per SM sub-partition, 4 per SM, at the SM clock
-    # sampled during the timed laps)
-    ninst = committed_instructions(args.workload, "fp32")
-    if ninst and t_kernel > 0 and clk and clk.get("sm_mhz"):
-        issue_peak = 152 * 4 * clk["sm_mhz"] * 1e6
-        roofline["issue"] = {"achieved": ninst / t_kernel, "peak": issue_peak, "unit": "warp-instructions/s",
-                             "frac": ninst / t_kernel / issue_peak, "instructions_per_launch": ninst,
-                             "peak_basis": "152 SMs x 4 issue slots x median SM clock under load"}
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        dt_cpu, cores = cpu_baseline(cfg, ions, lecs, args.cpu_steps)
-        cpu = {"value": n_p * args.cpu_steps / dt_cpu, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_steps} full laps of the workload (after 1 warm-up lap) on the OpenMP "
-                         "CPU restatement; the Fortran reference cannot be built (no Fortran compiler)"}
+    main_line = measure_workload(args.workload, args, ws, rank, local, args.steps, args.warmup, args.e2e_steps,
+                                 args.cpu_steps, args.sort_every, args.impl == "gb300" and not args.no_autotune
+                                 and args.sort_every == 0)
+    c3 = None
+    if args.workload == DEFAULT_WORKLOAD and not args.no_c3:
+        # the 3D order-2 target configuration (134 M particles): the same
+        # record, fewer laps (about 45 ms each)
+        c3 = measure_workload(C3_WORKLOAD, args, ws, rank, local, min(args.steps, 10), 3, 2,
+                              min(args.cpu_steps, 2), args.sort_every,
+                              args.impl == "gb300" and not args.no_autotune and args.sort_every == 0)
     ens = None
     if rank == 0 and not args.no_ensemble:
-        ens = run_ensemble(args, device)
+        ens = run_ensemble(args, local)
     shock = None
     if rank == 0 and not args.no_shock:
-        shock = run_shock(args, device)
+        shock = run_shock(args, local)
     if rank != 0:
         return
-    d = hist[-1] if len(hist) else None
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config, "fixed_point": fixed, "phase_ms_per_lap": phases,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": kps * args.steps, "ensemble": ens, "shock": shock,
-            "gauss_residual_last_lap": (float(np.sqrt(d[0] / d[1])) if d is not None and d[1] > 0 else None)}
+    line = {"metric": METRIC, "value": main_line["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": main_line["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    for k in ("config", "fixed_point", "phase_ms_per_lap", "roofline", "cpu_baseline", "e2e", "clocks",
+              "gpu_launches", "gauss", "gauss_residual_last_lap"):
+        line[k] = main_line[k]
+    line["c3"] = c3
+    line["ensemble"] = ens
+    line["shock"] = shock
     print(json.dumps(line), flush=True)
 
 

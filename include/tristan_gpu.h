@@ -46,8 +46,16 @@ extern "C" {
                              copy at code/fieldboundaries.F90:1938 */
 
 /* deposit modes, tg_config.deposit_mode */
-#define TG_DEPOSIT_FP32 0  /* FP32 shared-memory atomics, reference arithmetic */
-#define TG_DEPOSIT_FIXED 1 /* int64 fixed point: bit-reproducible currents */
+/* Both modes compute every Esirkepov contribution in FP32 in the
+   reference's order and sum a tile's contributions exactly in a fixed-point
+   shared-memory window; they differ in how the tile sums reach the global
+   currents. */
+#define TG_DEPOSIT_FP32 0  /* each tile sum rounded once to FP32 and added
+                              with FP32 global atomics (the summation order
+                              across tiles varies run to run) */
+#define TG_DEPOSIT_FIXED 1 /* tile sums added to int64 fixed-point global
+                              accumulators, converted to FP32 once per lap:
+                              bit-reproducible currents */
 
 /* sync masks */
 #define TG_SYNC_E 1u
@@ -100,9 +108,9 @@ typedef struct {
 
 /* Allocate the device domain: replaces allocate_fields
    (code/fields.F90:207-360) and allocate_particles
-   (code/particles.F90:286-341). TG_ERR_ARG for a domain with fewer than 8
-   interior cells along an axis (mx - nghost, my - nghost, and in 3D
-   mz - nghostz). */
+   (code/particles.F90:286-341). TG_ERR_ARG for a domain with fewer than
+   nghost/2 + 1 interior cells along an axis (mx - nghost, my - nghost, and
+   in 3D mz - nghostz): 3 at order 1, 4 at orders 2 and 3. */
 int tg_init(const tg_config *cfg, tg_ctx **out);
 /* Release everything (finalize, code/tristan.F90:38). */
 void tg_finalize(tg_ctx *ctx);
@@ -217,9 +225,15 @@ int tg_diag_history(tg_ctx *ctx, double *out, int32_t n);
    tg_step (and inside its captured graph). on != 0 enables it (graphs are
    re-captured; the last lap of each tg_step then runs outside the graph,
    since events recorded by graph nodes cannot be read back). tg_phase_times
-   returns, for the last lap of the last tg_step, the milliseconds of: [0] field update before the push, [1] the fused
-   push + deposit kernel, [2] field update after the push, [3] current fold,
-   filter and add_current, [4] tile sort, [5] FP64 diagnostics. */
+   returns, for the last lap of the last tg_step, the milliseconds of up to
+   TG_NPHASES phases, grouped as the reference's per-lap timers
+   (print_timers, code/communications.F90:242-326): [0] field update before
+   the push and [2] after it (with [5], "Field slv"), [1] the fused push +
+   deposit kernel ("Mover" + "Deposit"), [3] current fold ("Currnt exch"),
+   [4] filter passes ("Filter"), [5] add_current, with the shock's field
+   reset and injection when set ("Inject"), [6] tile sort ("Reorder"),
+   [7] FP64 diagnostics (no counterpart). A phase not run returns 0. */
+#define TG_NPHASES 8
 int tg_enable_timing(tg_ctx *ctx, int32_t on);
 int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases);
 
@@ -231,9 +245,12 @@ int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases);
    Its scratch is a fixed device array of 3 x TG_NOALLOC_MAX_CELLS floats
    held by every GPU that loads the library; larger grids are rejected with
    TG_ERR_ARG. The first call on a device looks the array up (make it before
-   any stream capture); calls that overlap on the GPU race on the shared
-   scratch. `stream` is a cudaStream_t (NULL: the default stream). Errors
-   are described by tg_last_error(NULL). */
+   any stream capture) and keeps its address for the life of the process:
+   after a cudaDeviceReset of that device the kept address is stale, so do
+   not call this entry point on a device that was reset. Calls that overlap
+   on the GPU race on the shared scratch. `stream` is a cudaStream_t (NULL:
+   the default stream). Errors are described by tg_last_error(NULL), whose
+   text is kept per host thread. */
 #define TG_NOALLOC_MAX_CELLS 1310720
 int tg_filter_noalloc(int32_t dims, int32_t mx, int32_t my, int32_t mz, int32_t nghost, int32_t nghostz,
                       const int32_t *periodic, int32_t ntimes, float *curx, float *cury, float *curz,

@@ -186,6 +186,8 @@ def load(openmp: bool = False) -> ctypes.CDLL:
             lib.to_maxwell_dist.restype = None
             lib.to_inject_plasma_region.argtypes = [P, K] + [ctypes.c_float] * 6
             lib.to_inject_plasma_region.restype = None
+            lib.to_inject_plasma_region3.argtypes = [P, K] + [ctypes.c_float] * 8
+            lib.to_inject_plasma_region3.restype = None
             for name in ("to_inject_particles_user", "to_particle_bc_user", "to_field_bc_user", "to_step_shock"):
                 getattr(lib, name).argtypes = [P, K]
                 getattr(lib, name).restype = None
@@ -303,6 +305,9 @@ class OracleSim:
 
     def inject_region(self, x1, x2, y1, y2, ppc, weight=1.0) -> None:
         self.lib.to_inject_plasma_region(self.ptr, self.kptr, x1, x2, y1, y2, ppc, weight)
+
+    def inject_region3(self, x1, x2, y1, y2, z1, z2, ppc, weight=1.0) -> None:
+        self.lib.to_inject_plasma_region3(self.ptr, self.kptr, x1, x2, y1, y2, z1, z2, ppc, weight)
 
     def step_shock(self, n: int = 1) -> None:
         for _ in range(n):

@@ -1120,7 +1120,12 @@ void to_diagnostics(const to_state *s, to_diag *out)
    double), returned as SEED/2^31 rounded to single */
 float to_random(double *dseed)
 {
-    double seed = fmod(16807.0 * *dseed, 2147483647.0);
+    double seed;
+    const int64_t si = (int64_t)*dseed;
+    if ((double)si == *dseed && si >= 0 && si < 2147483647LL)
+        seed = (double)((16807LL * si) % 2147483647LL); /* the same exact integer, without fmod */
+    else
+        seed = fmod(16807.0 * *dseed, 2147483647.0);
     *dseed = seed;
     return (float)(seed / 2147483648.0);
 }
@@ -1224,18 +1229,23 @@ void to_maxwell_dist(float gamma0, float cd, double *dseed, float *u, float *v, 
     const float beta_drift = copysignf(sqrtf(1.0f - 1.0f / (gm * gm)), gamma0);
     float rannum = to_random(dseed);
     if (rannum == 1.0f) rannum = to_random(dseed);
-    float gam = 0.0f;
-    for (int i = 1;; i++) {
-        int done = 0;
-        if (i == TO_PDF_SZ) {
-            gam = gt[TO_PDF_SZ - 1];
-            done = 1;
-        }
-        if (i < TO_PDF_SZ && rannum >= pt[i - 1] && rannum < pt[i]) {
-            gam = gt[i - 1] + (gt[i] - gt[i - 1]) / (pt[i] - pt[i - 1]) * (rannum - pt[i - 1]);
-            done = 1;
-        }
-        if (done) break;
+    /* The reference scans i = 1, 2, ... for the first interval with
+       pdf(i) <= rannum < pdf(i+1), stopping at i = pdf_sz. The table is
+       non-decreasing from pdf(1) = 0 <= rannum, so that interval is the one
+       whose upper end is the first entry above rannum: a binary search for
+       it gives the same i. */
+    int lo = 1, hi = TO_PDF_SZ; /* first 1-based i in [1, pdf_sz) with pt[i] > rannum, else pdf_sz */
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (pt[mid] > rannum) hi = mid;
+        else lo = mid + 1;
+    }
+    float gam;
+    if (lo >= TO_PDF_SZ) {
+        gam = gt[TO_PDF_SZ - 1];
+    } else {
+        const int i = lo;
+        gam = gt[i - 1] + (gt[i] - gt[i - 1]) / (pt[i] - pt[i - 1]) * (rannum - pt[i - 1]);
     }
     float pcosth = (2.0f * to_random(dseed) - 1.0f) * pcosthmult;
     if (sigma_nonzero) pcosth = 2.0f * to_random(dseed) - 1.0f;
@@ -1258,10 +1268,10 @@ void to_maxwell_dist(float gamma0, float cd, double *dseed, float *u, float *v, 
     *w = ptz / cd;
 }
 
-/* code/particles.F90:2549-2938 for 2D, drift along x, one electron per ion,
+/* code/particles.F90:2549-2938, drift along x, one electron per ion,
    no density profile: ions and electrons appended pairwise at one point */
-void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float ppc,
-                             float weight)
+static void inject_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float z1, float z2,
+                          float ppc, float weight)
 {
     const int ng = s->nghost, ngz = s->nghostz;
     const float gdi = k->gamma_drift;
@@ -1289,8 +1299,29 @@ void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float
         maxy = 0.0f;
         miny = 0.0f;
     }
-    const float maxz = 1.0f * (float)(ngz / 2 + 1) + 1.0f, minz = 1.0f * (float)(ngz / 2 + 1);
-    const float delta_z = maxz - minz;
+    float minz, maxz, delta_z;
+    if (s->dims == 2) {
+        maxz = 1.0f * (float)(ngz / 2 + 1) + 1.0f;
+        minz = 1.0f * (float)(ngz / 2 + 1);
+        delta_z = maxz - minz;
+    } else {
+        /* code/particles.F90:2695-2728: z as y, on this rank's slab */
+        const int64_t kglob_min = (ngz / 2 + 1) + s->mzcum, kglob_max = (s->mz - ngz / 2) + s->mzcum;
+        minz = 1.0f * (float)(ngz / 2 + 1);
+        maxz = 1.0f * (float)(ngz / 2 + 1);
+        if (z1 < (float)kglob_min) minz = 1.0f * (float)(ngz / 2 + 1);
+        if (z2 < (float)kglob_min) maxz = 1.0f * (float)(ngz / 2 + 1);
+        if (z1 >= (float)kglob_max) minz = (float)s->mz - 1.0f * (float)(ngz / 2);
+        if (z2 >= (float)kglob_max) maxz = (float)s->mz - 1.0f * (float)(ngz / 2);
+        if (z1 >= (float)kglob_min && z1 < (float)kglob_max) minz = z1 - (float)s->mzcum;
+        if (z2 >= (float)kglob_min && z2 < (float)kglob_max) maxz = z2 - (float)s->mzcum;
+        delta_z = maxz - minz;
+        if (maxz == 0.0f || minz == 0.0f) {
+            delta_z = 0.0f;
+            maxz = 0.0f;
+            minz = 0.0f;
+        }
+    }
     float numps = (0.5f * ppc) * delta_z * delta_y * delta_x;
     if (numps < 10.0f) numps = numps != 0.0f ? to_poisson(numps, &k->dseed) : 0.0f;
     else numps = (float)(int32_t)ceilf(numps);
@@ -1322,6 +1353,19 @@ void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float
         pe->splitlev = 1;
     }
     k->injected += n;
+}
+
+void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float ppc,
+                             float weight)
+{
+    inject_region(s, k, x1, x2, y1, y2, 0.0f, 0.0f, ppc, weight);
+}
+
+/* the same with the z range of a 3D build (z1, z2 ignored in 2D) */
+void to_inject_plasma_region3(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float z1, float z2,
+                              float ppc, float weight)
+{
+    inject_region(s, k, x1, x2, y1, y2, z1, z2, ppc, weight);
 }
 
 /* inject_from_wall (code/particles.F90:2439-2538) for a wall normal to x at

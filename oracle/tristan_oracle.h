@@ -192,9 +192,12 @@ float to_poisson(float numps, double *dseed);                     /* aux.F90:110
 void to_init_maxw_table(float delgam, int dims, float pcosthmult, float *gamma_table, float *pdf_table);
 void to_maxwell_dist(float gamma0, float cd, double *dseed, float *u, float *v, float *w,
                      const float *gamma_table, const float *pdf_table, float pcosthmult, int sigma_nonzero);
-/* inject_plasma_region for 2D, drift along x (direction 1) */
+/* inject_plasma_region, drift along x (direction 1); the 3D form takes the
+   z range (code/particles.F90:2695-2728) */
 void to_inject_plasma_region(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float ppc,
                              float weight);
+void to_inject_plasma_region3(to_state *s, to_shock *k, float x1, float x2, float y1, float y2, float z1, float z2,
+                              float ppc, float weight);
 void to_inject_particles_user(to_state *s, to_shock *k);          /* :364-395 */
 void to_particle_bc_user(to_state *s, to_shock *k);               /* :514-611 */
 void to_field_bc_user(to_state *s, const to_shock *k);            /* :460-488 */

@@ -38,7 +38,7 @@ BASE = dict(dims=2, order=3, nx=32, ny=32, maxhlf=1024)
     (dict(nghost=5), "nghost"),
     (dict(mz=3), "mz = 1"),
     (dict(mx=8, my=8), "too small"),
-    (dict(my=4 + 7), "too small"),  # 4 interior rows under 7 ghost rows
+    (dict(my=3 + 7), "too small"),  # 3 interior rows: the images of ghost rows are ghost rows
     (dict(maxhlf=0), "maxhlf"),
     (dict(dims=4), "dims"),
 ])

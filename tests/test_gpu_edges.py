@@ -6,6 +6,8 @@ import pytest
 
 import oracle
 from test_gpu_parity import assert_fields_equal, assert_particles_equal, beams, random_fields, small_cfg
+from tristan_gb300 import setups
+from tristan_gb300.config import SimConfig
 
 pytestmark = pytest.mark.gpu
 
@@ -71,3 +73,25 @@ def test_bad_arguments_return_status():
     g.sync_to_host()
     assert len(g.ions) == len(ions)
     g.close()
+
+
+def test_phase_timers_follow_the_reference_timer_groups():
+    """tg_phase_times splits a timed lap as the reference's per-lap timers
+    (Field slv, Mover + Deposit, Currnt exch, Filter, Reorder): every phase
+    that runs has a positive time"""
+    from tristan_gb300.gpu import PHASES, GpuSim
+    cfg = SimConfig(dims=2, order=3, nx=64, ny=48, ppc0=8.0, c_omp=4.0, ntimes=4, sort_every=1, diag_every=1)
+    ions, lecs = setups.load_beams(cfg, seed=3)
+    setups.with_capacity(cfg, len(ions), len(lecs))
+    g = GpuSim(cfg)
+    try:
+        g.set_particles(ions, lecs)
+        g.step(2)
+        g.enable_timing(True)
+        g.step_timed(4)
+        ph = g.phase_times()
+    finally:
+        g.close()
+    assert tuple(ph) == PHASES
+    for k in PHASES:
+        assert ph[k] > 0.0, (k, ph[k])

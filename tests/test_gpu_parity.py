@@ -125,6 +125,44 @@ def test_fold_bit_exact(dims, order, q5):
     g.close()
 
 
+# thin local grids: fewer interior cells than ghost cells along an axis, so
+# the fold's two target slabs overlap and are added in order, as the
+# reference does (code/fieldboundaries.F90:1797-1812); the smallest is
+# nghost/2 + 1 cells
+THIN = [(2, 3, dict(nx=64, ny=4)), (2, 1, dict(nx=40, ny=3)), (2, 2, dict(nx=5, ny=24)),
+        (3, 2, dict(nx=12, ny=4, nz=10)), (3, 3, dict(nx=10, ny=10, nz=4))]
+
+
+@pytest.mark.parametrize("dims,order,grid", THIN)
+@pytest.mark.parametrize("q5", [False, True])
+def test_fold_thin_grids_bit_exact(dims, order, grid, q5):
+    cfg = small_cfg(dims, order, maxhlf=16, quirks=oracle.QUIRK_Q5_LHS if q5 else 0, **grid)
+    f = random_fields(cfg, np.random.default_rng(21), names=("curx", "cury", "curz"))
+    o, g = pair(cfg, fields=f)
+    g.exchange_current()
+    o.call("to_exchange_current")
+    g.sync_to_host()
+    assert_fields_equal(o, g, ("curx", "cury", "curz"))
+    g.close()
+
+
+@pytest.mark.parametrize("dims,order,grid", THIN)
+def test_laps_thin_grids_fixed_point_bit_exact(dims, order, grid):
+    """whole laps on thin grids (the 64 x 4 order-3 box among them): every
+    field and particle bit-exact in fixed point"""
+    cfg = small_cfg(dims, order, fixed=1, **grid)
+    ions, lecs = beams(cfg)
+    f = random_fields(cfg, np.random.default_rng(22), scale=0.02)
+    o, g = pair(cfg, ions, lecs, f)
+    g.step(8)
+    o.step(8)
+    g.sync_to_host()
+    assert_fields_equal(o, g, ("ex", "ey", "ez", "bx", "by", "bz", "curx", "cury", "curz"))
+    assert_particles_equal(g.ions, o.ions)
+    assert_particles_equal(g.lecs, o.lecs)
+    g.close()
+
+
 @pytest.mark.parametrize("dims,order", CASES)
 @pytest.mark.parametrize("ntimes", [3, 4])
 def test_filter_bit_exact(dims, order, ntimes):

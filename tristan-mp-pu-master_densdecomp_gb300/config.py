@@ -38,7 +38,8 @@ class SimConfig:
     ntimes: int = 4
     corr: float = 1.025
     periodic: tuple = (1, 1, 1)
-    # deposit: 0 = FP32 atomics, 1 = int64 fixed point
+    # deposit: 0 = tile sums rounded to FP32 (FP32 global atomics),
+    # 1 = int64 fixed point (bit-reproducible)
     fixed: int = 0
     quirks: int = 0
     external_fields: int = 0

@@ -15,14 +15,29 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "tg_internal.cuh"
 #include "tg_spectrum.cuh"
 
 using namespace tg;
 
+// An NVTX range over one host entry point, named after the reference
+// subroutine it replaces, so a timeline (nsys, ncu --nvtx) shows the main
+// loop's phases; costs nothing when no tool is attached.
+namespace {
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+}  // namespace
+#define TG_RANGE(name) NvtxRange tg_nvtx_range_(name)
+
 static thread_local char g_init_error[512];
 
-#define TG_NPHASES 6  // fields before the push, particles, fields after, current, sort, diagnostics
+// phase timers: TG_NPHASES of tristan_gpu.h
 
 struct tg_ctx {
     tg_config cfg;
@@ -167,13 +182,14 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.ng = c.nghost;
     g.ngz = c.nghostz;
     const int nx = c.mx - g.ng, ny = c.my - g.ng, nz = c.dims == 3 ? c.mz - g.ngz : 1;
-    // at least 8 interior cells per axis, no fewer than the widest ghost band
-    // (7 cells): the current fold adds both ghost slabs of an axis in one
-    // launch, and with fewer interior cells than ghost cells the two slabs'
-    // target layers overlap (the reference folds one slab after the other)
-    if (nx < 8 || ny < 8 || nz < 1 || (c.dims == 3 && nz < 8))
-        return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells; at least 8 per axis)", nx, ny,
-                         nz);
+    // more interior cells per axis than half the ghost band (nghost/2 + 1:
+    // 3 at order 1, 4 at orders 2 and 3): below that the periodic images of
+    // the ghost layers are themselves ghost layers, and the current fold's
+    // first slab would read cells it writes
+    const int nmin = g.ng / 2 + 1, nzmin = c.dims == 3 ? g.ngz / 2 + 1 : 1;
+    if (nx < nmin || ny < nmin || nz < nzmin)
+        return geom_fail(err, errlen, "grid too small (%d x %d x %d interior cells; at least %d per axis)", nx, ny,
+                         nz, nmin);
     g.lot = (long long)c.mx * c.my * c.mz;
     if (g.lot >= (1LL << 31)) return geom_fail(err, errlen, "grid of %lld cells exceeds int32 cell indices", g.lot);
     g.sy = c.mx;
@@ -536,6 +552,7 @@ static void *host_view(tg_ctx *ctx, void *h) {
 }
 
 extern "C" int tg_sync_from_host(tg_ctx *ctx, unsigned mask) {
+    TG_RANGE("tg_sync_from_host");
     if (!ctx) return TG_ERR_ARG;
     const size_t lot = (size_t)ctx->g.lot;
     const int groups[3][4] = {{0, 1, 2, (int)TG_SYNC_E}, {3, 4, 5, (int)TG_SYNC_B}, {6, 7, 8, (int)TG_SYNC_CUR}};
@@ -612,6 +629,7 @@ extern "C" int tg_get_counts(tg_ctx *ctx, int64_t *ions, int64_t *lecs) {
 }
 
 extern "C" int tg_sync_to_host(tg_ctx *ctx, unsigned mask) {
+    TG_RANGE("tg_sync_to_host");
     if (!ctx) return TG_ERR_ARG;
     const size_t lot = (size_t)ctx->g.lot;
     const int groups[3][4] = {{0, 1, 2, (int)TG_SYNC_E}, {3, 4, 5, (int)TG_SYNC_B}, {6, 7, 8, (int)TG_SYNC_CUR}};
@@ -653,30 +671,35 @@ extern "C" int tg_sync_to_host(tg_ctx *ctx, unsigned mask) {
 // per-subroutine entry points
 // ---------------------------------------------------------------------------
 extern "C" int tg_bc_b1(tg_ctx *ctx) {
+    TG_RANGE("bc_b1");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_ghost(ctx->g, ctx->f[3], ctx->f[4], ctx->f[5], GHOST_BC, ctx->st));
     return TG_OK;
 }
 
 extern "C" int tg_bc_e1(tg_ctx *ctx) {
+    TG_RANGE("bc_e1");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_ghost(ctx->g, ctx->f[0], ctx->f[1], ctx->f[2], GHOST_BC, ctx->st));
     return TG_OK;
 }
 
 extern "C" int tg_advance_b_half(tg_ctx *ctx) {
+    TG_RANGE("advance_Bhalfstep");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_advance_b(ctx->g, ctx->P, ctx->f, ctx->st));
     return TG_OK;
 }
 
 extern "C" int tg_advance_e(tg_ctx *ctx) {
+    TG_RANGE("advance_Efield");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_advance_e(ctx->g, ctx->P, ctx->f, ctx->st));
     return TG_OK;
 }
 
 extern "C" int tg_move(tg_ctx *ctx) {
+    TG_RANGE("move_particles");
     if (!ctx) return TG_ERR_ARG;
     FieldPtrs fp;
     fp.ex = ctx->f[0]; fp.ey = ctx->f[1]; fp.ez = ctx->f[2];
@@ -693,6 +716,7 @@ extern "C" int tg_move(tg_ctx *ctx) {
 }
 
 extern "C" int tg_reset_currents(tg_ctx *ctx) {
+    TG_RANGE("reset_currents");
     if (!ctx) return TG_ERR_ARG;
     const size_t lot = (size_t)ctx->g.lot;
     for (int a = 6; a < 9; a++) CK(cudaMemsetAsync(ctx->f[a], 0, lot * 4, ctx->st));
@@ -700,6 +724,7 @@ extern "C" int tg_reset_currents(tg_ctx *ctx) {
 }
 
 extern "C" int tg_deposit(tg_ctx *ctx) {
+    TG_RANGE("deposit_particles");
     if (!ctx) return TG_ERR_ARG;
     int r = ensure_sorted(ctx);
     if (r) return r;
@@ -716,6 +741,7 @@ extern "C" int tg_deposit(tg_ctx *ctx) {
 }
 
 extern "C" int tg_fold_currents(tg_ctx *ctx) {
+    TG_RANGE("exchange_current");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_fold(ctx->g, ctx->P, ctx->f + 6, ctx->st));
     return TG_OK;
@@ -735,17 +761,20 @@ static int filter_passes(tg_ctx *ctx) {
 }
 
 extern "C" int tg_filter(tg_ctx *ctx) {
+    TG_RANGE("apply_filter1_opt");
     if (!ctx) return TG_ERR_ARG;
     return filter_passes(ctx);
 }
 
 extern "C" int tg_add_current(tg_ctx *ctx) {
+    TG_RANGE("add_current");
     if (!ctx) return TG_ERR_ARG;
     CK(launch_add_current(ctx->g, ctx->f, ctx->st));
     return TG_OK;
 }
 
 extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
+    TG_RANGE("reorder_particles");
     if (!ctx) return TG_ERR_ARG;
     if (!force) {
         // code/particles.F90:398-400
@@ -1148,10 +1177,14 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
         CK(launch_fixed_to_float(g, ctx->P, ctx->fix, cur3, st)); k++;
     }
     // exchange_current; apply_filter1_opt; add_current (:201-242)
-    CK(launch_fold(g, ctx->P, ctx->f + 6, st)); k += g.dims;
+    CK(launch_fold(g, ctx->P, ctx->f + 6, st)); k += fold_launches(g);
+    CK(mark(ctx, li, 3, 1));
+    CK(mark(ctx, li, 4, 0));
     int r = filter_passes(ctx);
     if (r) return r;
     k += ctx->cfg.ntimes;
+    CK(mark(ctx, li, 4, 1));
+    CK(mark(ctx, li, 5, 0));
     CK(launch_add_current(g, ctx->f, st)); k++;
     if (ctx->shock_on) {
         // field_bc_user; inject_particles_user (:242-262); the injected
@@ -1161,7 +1194,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
         if (rr) return rr;
         k += 4;
     }
-    CK(mark(ctx, li, 3, 1));
+    CK(mark(ctx, li, 5, 1));
     if (pipe) {
         // the fields are final here (the diagnostics only read them): they
         // go home while the diagnostics run
@@ -1171,18 +1204,18 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
             CK(cudaMemcpyAsync(ctx->hf[f9], ctx->f[f9], (size_t)g.lot * 4, cudaMemcpyDeviceToHost, pipe->down));
     }
     if (sort_now && !pipe) {
-        CK(mark(ctx, li, 4, 0));
+        CK(mark(ctx, li, 6, 0));
         int rr = sort_all(ctx, true);
         if (rr) return rr;
         k += 4;
-        CK(mark(ctx, li, 4, 1));
+        CK(mark(ctx, li, 6, 1));
     }
     if (ctx->cfg.diag_every > 0) {
-        CK(mark(ctx, li, 5, 0));
+        CK(mark(ctx, li, 7, 0));
         int rr = run_diag(ctx, true, pipe);
         if (rr) return rr;
         k += 4 + ctx->g.dims * ctx->cfg.ntimes + (pipe ? pipe->parts - 1 : 0);
-        CK(mark(ctx, li, 5, 1));
+        CK(mark(ctx, li, 7, 1));
     }
     *nk = k;
     return TG_OK;
@@ -1211,6 +1244,7 @@ static int capture_cycle(tg_ctx *ctx, int start_par) {
 }
 
 extern "C" int tg_step(tg_ctx *ctx, int32_t nsteps) {
+    TG_RANGE("tg_step (main loop laps)");
     if (!ctx || nsteps < 0) return TG_ERR_ARG;
     int r = ensure_sorted(ctx);
     if (r) return r;
@@ -1446,6 +1480,7 @@ extern "C" int tg_pin_host(tg_ctx *ctx) {
 }
 
 extern "C" int tg_step_host(tg_ctx *ctx, int32_t nsteps) {
+    TG_RANGE("tg_step_host (main loop laps, host state)");
     if (!ctx || nsteps < 0) return TG_ERR_ARG;
     for (int l = 0; l < nsteps; l++) {
         int r = host_lap(ctx);
@@ -1498,6 +1533,7 @@ extern "C" int tg_phase_times(tg_ctx *ctx, float *ms, int32_t nphases) {
 }
 
 extern "C" int tg_diag_fp64(tg_ctx *ctx, tg_diag *out) {
+    TG_RANGE("tg_diag_fp64");
     if (!ctx || !out) return TG_ERR_ARG;
     // injected particles may sit past the tile ranges since the last sort
     if (ctx->shock_on && ctx->cfg.sort_every > 1) ctx->dirty = true;

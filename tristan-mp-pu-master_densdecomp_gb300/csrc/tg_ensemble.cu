@@ -408,6 +408,11 @@ extern "C" int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out) {
             r = efail(E, TG_ERR_ARG, "box %d: maxhlf must be in [1, 2^31)", b);
         else if (build_geom(c, E->g[b], why, sizeof why) != TG_OK)
             r = efail(E, TG_ERR_ARG, "box %d: %s", b, why);
+        // the batched fold adds both ghost slabs of an axis in one launch,
+        // which needs disjoint target slabs: nghost interior cells per axis
+        else if (!fold_in_one_pass(E->g[b], 0) || !fold_in_one_pass(E->g[b], 1))
+            r = efail(E, TG_ERR_ARG, "box %d: ensemble boxes need at least %d interior cells per axis", b,
+                      E->g[b].ng);
         if (!r) build_params(c, E->P[b]);
     }
     if (r) {

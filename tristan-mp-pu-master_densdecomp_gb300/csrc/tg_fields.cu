@@ -123,15 +123,17 @@ cudaError_t launch_add_current(const Geom &g, float *const *f, cudaStream_t st) 
 
 // ---------------------------------------------------------------------------
 // exchange_current for one rank (code/fieldboundaries.F90:1768-2189):
-// per axis, cur(ng/2+1..ng) += cur(m-ng/2..m) and
-// cur(m-(ng-1)..m-(ng/2+1)) += cur(1..ng/2). Targets and sources are
-// disjoint, so one thread per target cell. Axis order x, y, z.
+// per axis, cur(ng/2+1..ng) += cur(m-ng/2..m), then
+// cur(m-(ng-1)..m-(ng/2+1)) += cur(1..ng/2). Axis order x, y, z. One
+// thread per target cell; an axis with at least nghost interior cells has
+// disjoint target slabs and folds in one launch, a thinner one in two
+// ordered launches (slab 1, then slab 2), as the reference adds them.
 // ---------------------------------------------------------------------------
-__global__ void k_fold(Geom g, int axis, int m, int ng, float *cx, float *cy, float *cz, int q5) {
-    const long long total = fold_cells(g, axis);
+__global__ void k_fold(Geom g, int axis, int m, int ng, float *cx, float *cy, float *cz, int q5, int slab) {
+    const long long total = fold_cells(g, axis, slab);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x)
-        fold_one(g, axis, m, ng, cx, cy, cz, q5, t);
+        fold_one(g, axis, m, ng, cx, cy, cz, q5, t, slab);
 }
 
 cudaError_t launch_fold(const Geom &g, const Params &P, float *const *cur, cudaStream_t st) {
@@ -140,13 +142,23 @@ cudaError_t launch_fold(const Geom &g, const Params &P, float *const *cur, cudaS
         if (!g.per[axis]) continue;
         const int m = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
         const int ng = axis == 2 ? g.ngz : g.ng;
-        const long long total = fold_cells(g, axis);
         const int q5 = (axis == 1) && (P.quirks & TG_QUIRK_Q5_LHS);
-        k_fold<<<blocks_for(total, 256), 256, 0, st>>>(g, axis, m, ng, cur[0], cur[1], cur[2], q5);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+        const bool one = fold_in_one_pass(g, axis);
+        for (int slab = one ? -1 : 0; slab < (one ? 0 : 2); slab++) {
+            const long long total = fold_cells(g, axis, slab);
+            k_fold<<<blocks_for(total, 256), 256, 0, st>>>(g, axis, m, ng, cur[0], cur[1], cur[2], q5, slab);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
     }
     return cudaSuccess;
+}
+
+int fold_launches(const Geom &g) {
+    int n = 0;
+    for (int axis = 0; axis < g.dims; axis++)
+        if (g.per[axis]) n += fold_in_one_pass(g, axis) ? 1 : 2;
+    return n;
 }
 
 template <int DIM>

@@ -168,13 +168,20 @@ __device__ __forceinline__ void advance_e_one(const Geom &g, const Box &b_, floa
     }
 }
 
+// One target cell of the current fold of one axis. The reference snapshots
+// both source slabs first, then adds slab 1 (cur(ng/2+1 : ng) +=
+// cur(m-ng/2 : m)) and after it slab 2 (cur(m-(ng-1) : m-(ng/2+1)) +=
+// cur(1 : ng/2)) (code/fieldboundaries.F90:1797-1812). slab < 0 covers
+// both slabs in one index range (t < nb1 faces: slab 1), for grids whose
+// two target ranges are disjoint; slab 0 / 1 index one slab alone, for the
+// ordered two-launch form.
 __device__ __forceinline__ void fold_one(const Geom &g, int axis, int m, int ng, float *cx, float *cy, float *cz,
-                                         int q5, long long t) {
+                                         int q5, long long t, int slab = -1) {
     const int nb1 = ng / 2 + 1;
     const int n1 = axis == 0 ? g.my : g.mx;  // first face extent
     const int n2 = axis == 2 ? g.my : g.mz;  // second face extent
     const long long face = (long long)n1 * n2;
-    const int layer = (int)(t / face);
+    const int layer = (int)(t / face) + (slab == 1 ? nb1 : 0);
     const long long f = t % face;
     const int p = (int)(f % n1) + 1, q = (int)(f / n1) + 1;
     (void)n2;
@@ -198,11 +205,24 @@ __device__ __forceinline__ void fold_one(const Geom &g, int axis, int m, int ng,
     cz[lt] = cz[lt] + cz[ls];
 }
 
-// cells written by one axis of the fold: both slabs of a face
-__host__ __device__ inline long long fold_cells(const Geom &g, int axis) {
+// cells written by one axis of the fold: both slabs of a face (slab < 0),
+// or slab 0 (nghost/2 + 1 layers) or slab 1 (nghost/2 layers) alone
+__host__ __device__ inline long long fold_cells(const Geom &g, int axis, int slab = -1) {
     const int ng = axis == 2 ? g.ngz : g.ng;
     const int n1 = axis == 0 ? g.my : g.mx, n2 = axis == 2 ? g.my : g.mz;
-    return (long long)n1 * n2 * ng;
+    const int layers = slab < 0 ? ng : slab == 0 ? ng / 2 + 1 : ng / 2;
+    return (long long)n1 * n2 * layers;
+}
+
+// The two slabs' target layers (nghost/2+1 .. nghost and m-(nghost-1) ..
+// m-(nghost/2+1)) are disjoint when the axis has at least nghost interior
+// cells; below that they overlap and the slabs must be added in order.
+// Each slab's sources never overlap a target layer of the same or the
+// earlier slab while the axis has more than nghost/2 interior cells.
+__host__ __device__ inline bool fold_in_one_pass(const Geom &g, int axis) {
+    const int m = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
+    const int ng = axis == 2 ? g.ngz : g.ng;
+    return m - ng >= ng;
 }
 
 // ---------------------------------------------------------------------------

@@ -527,6 +527,8 @@ cudaError_t launch_advance_b(const Geom &g, const Params &P, float *const *f, cu
 cudaError_t launch_advance_e(const Geom &g, const Params &P, float *const *f, cudaStream_t st);
 cudaError_t launch_add_current(const Geom &g, float *const *f, cudaStream_t st);
 cudaError_t launch_fold(const Geom &g, const Params &P, float *const *cur, cudaStream_t st);
+// kernel launches of one launch_fold
+int fold_launches(const Geom &g);
 cudaError_t launch_filter_pass(const Geom &g, float *const *in, float *const *out, cudaStream_t st);
 cudaError_t launch_primal(const Geom &g, float *const *f, float *const *pf, cudaStream_t st);
 cudaError_t launch_fixed_to_float(const Geom &g, const Params &P, unsigned long long *const *fx, float *const *cur,

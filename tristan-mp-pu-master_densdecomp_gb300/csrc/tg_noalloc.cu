@@ -15,8 +15,11 @@
 //    TG_NOALLOC_MAX_CELLS floats, 15.7 MB) until the process exits;
 //  * grids above TG_NOALLOC_MAX_CELLS cells (mx*my*mz) are rejected;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture;
+//    cudaGetSymbolAddress (with that device current) and keeps it for the
+//    life of the process; make that first call before any stream capture.
+//    A cudaDeviceReset of that device makes the kept address stale: the
+//    entry point must not be called on a device after a reset;
+//  * error text goes to the per-thread message of tg_last_error(NULL);
 //  * all calls share the one array: calls that overlap on the GPU (two
 //    streams, or two host threads) race on it. Every pass writes every
 //    scratch cell it later reads, so nothing needs clearing between calls.

@@ -621,8 +621,13 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     const double walloc = (a.shock && a.wall) ? a.shock->walloc : -1.0e300;
     const double x2in = a.shock ? a.shock->x2in : a.P.x2in;
     // particles since the last flush; the window is exact for up to 65536
-    // contributions per cell, i.e. 65536 particles (every bound is uniform
-    // across the CTA, so the barriers below are reached by all threads)
+    // contributions per cell. The Esirkepov stencil adds one contribution
+    // per cell and component; a particle reflected by the wall adds up to
+    // four more (two zigzag segments, each touching a cell twice when both
+    // ends share it), so wall laps flush every 65536 / 5 particles (every
+    // bound is uniform across the CTA, so the barriers below are reached by
+    // all threads)
+    const int batch = a.wall ? TG_WIN_BATCH / 5 : TG_WIN_BATCH;
     int since = 0;
 #pragma unroll 1
     for (int s = a.only == 2 ? 1 : 0; s < (a.only == 1 ? 1 : 2); s++) {
@@ -632,13 +637,13 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
         const float qs = a.P.qs[s];
 #pragma unroll 1
         for (int b0 = beg; b0 < end;) {
-            const int b1 = min(end, b0 + (TG_WIN_BATCH - since));
+            const int b1 = min(end, b0 + (batch - since));
 #pragma unroll 1
             for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x)
                 particle_step<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, sink, sp, n, a.newcount[s], qm, qs, walloc, x2in);
             since += b1 - b0;
             b0 = b1;
-            if (DEPOSIT && since == TG_WIN_BATCH) {
+            if (DEPOSIT && since == batch) {
                 __syncthreads();
                 flush_window<FIXED>(a, sink, winlo, winhi);
                 __syncthreads();

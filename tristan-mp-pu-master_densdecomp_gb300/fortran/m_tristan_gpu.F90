@@ -3,25 +3,42 @@
 ! the GB300 C-ABI (include/tristan_gpu.h).
 !
 ! The reference main loop (code/tristanmainloop.F90:107-344) calls
-! argument-less module subroutines. This module gives the same names and
-! forwards to libtristan_gpu.so; the module-global arrays of m_fields and
-! m_particles are registered once with tg_bind_fields / tg_bind_particles
-! and synchronised only around host-side work (Diagnostics, output, restart,
-! host user hooks). Compile with the reference's -DtwoD/-Dddk flags and link
-! -ltristan_gpu. Not compiled in this repository (no Fortran compiler).
+! argument-less module subroutines. This module exports the same names
+! (bc_b1, bc_e1, bc_b2, bc_e2, advance_Bhalfstep, advance_Efield,
+! move_particles, reset_currents, deposit_particles, exchange_current,
+! apply_filter1_opt, add_current, reorder_particles and the shock setup's
+! particle_bc_user, field_bc_user, inject_particles_user) and forwards them
+! to libtristan_gpu.so, so the lap body compiles unchanged: the module that
+! holds mainloop adds `use m_tristan_gpu` and renames the CPU versions away
+! on its existing use lines (e.g. `use m_fields, cpu_add_current =>
+! add_current`). The module-global arrays of m_fields and m_particles are
+! registered once with tg_bind_fields / tg_bind_particles and synchronised
+! only around host-side work: reorder_particles, the last hot call of a
+! lap, brings the device state home before a lap whose Diagnostics writes
+! output (every gpu_sync_every laps, set by tg_start). Compile with the
+! reference's -DtwoD/-Dddk flags and link -ltristan_gpu. Not compiled in
+! this repository (no Fortran compiler).
 !
+! The CPU subroutines this module replaces are renamed away on its own use
+! lines, so the local procedures below can carry their names.
 #ifdef twoD
 module m_tristan_gpu
+  use m_globaldata
   use m_system
   use m_aux
-  use m_fields
-  use m_particles
+  use m_communications
+  use m_fields, cpu_advance_Efield => advance_Efield, cpu_advance_Bhalfstep => advance_Bhalfstep, &
+                cpu_add_current => add_current, cpu_reset_currents => reset_currents
+  use m_particles, cpu_reorder_particles => reorder_particles
 #else
 module m_tristan_gpu_3d
+  use m_globaldata_3d
   use m_system_3d
   use m_aux_3d
-  use m_fields_3d
-  use m_particles_3d
+  use m_communications_3d
+  use m_fields_3d, cpu_advance_Efield => advance_Efield, cpu_advance_Bhalfstep => advance_Bhalfstep, &
+                   cpu_add_current => add_current, cpu_reset_currents => reset_currents
+  use m_particles_3d, cpu_reorder_particles => reorder_particles
 #endif
   use iso_c_binding
   implicit none
@@ -280,11 +297,15 @@ module m_tristan_gpu_3d
   type(c_ptr), save :: ctx = c_null_ptr
   integer(c_int), parameter :: SYNC_E = 1, SYNC_B = 2, SYNC_CUR = 4, SYNC_PARTICLES = 8, SYNC_ALL = 15
 
-  public :: tg_start, tg_stop, tg_download, tg_upload, tg_pin, tg_parts, &
-            gpu_bc_b1, gpu_bc_e1, gpu_advance_Bhalfstep, gpu_advance_Efield, gpu_move_particles, &
-            gpu_reset_currents, gpu_deposit_particles, gpu_exchange_current, gpu_apply_filter1_opt, &
-            gpu_add_current, gpu_reorder_particles, gpu_step, gpu_step_host, &
-            gpu_particle_bc_user, gpu_field_bc_user, gpu_inject_particles_user, &
+  ! laps between downloads of the device state (0: never), so that the
+  ! host arrays are current when Diagnostics writes output
+  integer, save :: gpu_sync_every = 0
+
+  public :: tg_start, tg_stop, tg_download, tg_upload, tg_pin, tg_parts, gpu_sync_every, &
+            bc_b1, bc_e1, bc_b2, bc_e2, advance_Bhalfstep, advance_Efield, move_particles, &
+            reset_currents, deposit_particles, exchange_current, apply_filter1_opt, &
+            add_current, reorder_particles, gpu_step, gpu_step_host, &
+            particle_bc_user, field_bc_user, inject_particles_user, &
             gpu_write_restart, gpu_read_restart, gpu_meanq, gpu_spectrum_bins, gpu_spectrum, gpu_output_var, &
             gpu_output_particles, tg_diag, gpu_diagnostics, gpu_counts, gpu_synchronize, gpu_output_dims, &
             gpu_spectrum2d_bins, gpu_spectrum2d
@@ -308,8 +329,8 @@ contains
   end subroutine check
 
   ! after read_input_* and allocate_*: the device mirror of one rank's domain
-  subroutine tg_start(deposit_mode, sort_every)
-    integer, intent(in) :: deposit_mode, sort_every
+  subroutine tg_start(deposit_mode, sort_every, sync_every)
+    integer, intent(in) :: deposit_mode, sort_every, sync_every
     type(tg_config) :: cfg
     cfg%dims = merge(2, 3, mz == 1)
 #ifdef dd1
@@ -341,6 +362,7 @@ contains
                c_loc(curx), c_loc(cury), c_loc(curz)), "tg_bind_fields")
     call check(tg_bind_particles(ctx, c_loc(p), c_loc(ions), c_loc(lecs)), "tg_bind_particles")
     call check(tg_sync_from_host(ctx, SYNC_ALL), "tg_sync_from_host")
+    gpu_sync_every = sync_every
   end subroutine tg_start
 
   subroutine tg_stop()
@@ -369,48 +391,61 @@ contains
     call check(tg_sync_from_host(ctx, SYNC_ALL), "tg_sync_from_host")
   end subroutine tg_upload
 
-  subroutine gpu_bc_b1()
+  ! the lap body's hot calls (code/tristanmainloop.F90:117-303)
+  subroutine bc_b1()
     call check(tg_bc_b1(ctx), "bc_b1")
   end subroutine
-  subroutine gpu_bc_e1()
+  subroutine bc_e1()
     call check(tg_bc_e1(ctx), "bc_e1")
   end subroutine
-  subroutine gpu_advance_Bhalfstep()
+  ! without radiation boundaries bc_b2 / bc_e2 are the periodic copies
+  subroutine bc_b2()
+    call check(tg_bc_b1(ctx), "bc_b2")
+  end subroutine
+  subroutine bc_e2()
+    call check(tg_bc_e1(ctx), "bc_e2")
+  end subroutine
+  subroutine advance_Bhalfstep()
     call check(tg_advance_b_half(ctx), "advance_Bhalfstep")
   end subroutine
-  subroutine gpu_advance_Efield()
+  subroutine advance_Efield()
     call check(tg_advance_e(ctx), "advance_Efield")
   end subroutine
-  subroutine gpu_move_particles()
+  subroutine move_particles()
     call check(tg_move(ctx), "move_particles")
   end subroutine
-  subroutine gpu_reset_currents()
+  subroutine reset_currents()
     call check(tg_reset_currents(ctx), "reset_currents")
   end subroutine
-  subroutine gpu_deposit_particles()
+  subroutine deposit_particles()
     call check(tg_deposit(ctx), "deposit_particles")
   end subroutine
-  subroutine gpu_exchange_current()
+  subroutine exchange_current()
     call check(tg_fold_currents(ctx), "exchange_current")
   end subroutine
-  subroutine gpu_apply_filter1_opt()
+  subroutine apply_filter1_opt()
     call check(tg_filter(ctx), "apply_filter1_opt")
   end subroutine
-  subroutine gpu_add_current()
+  subroutine add_current()
     call check(tg_add_current(ctx), "add_current")
   end subroutine
-  subroutine gpu_reorder_particles()
+  ! the last hot call of a lap: the reorder on the reference's cadence, then
+  ! the device state home when the next lap's Diagnostics writes output
+  subroutine reorder_particles()
     call check(tg_reorder(ctx, int(lap, c_int32_t), 0_c_int32_t), "reorder_particles")
+    if (gpu_sync_every > 0) then
+       if (modulo(lap + 1, gpu_sync_every) == 0) call tg_download()
+    endif
   end subroutine
 
   ! the shock's user hooks on the device (after tg_shock_init)
-  subroutine gpu_particle_bc_user()
+  subroutine particle_bc_user()
     call check(tg_particle_bc(ctx), "particle_bc_user")
   end subroutine
-  subroutine gpu_field_bc_user()
+  subroutine field_bc_user()
     call check(tg_field_bc(ctx), "field_bc_user")
   end subroutine
-  subroutine gpu_inject_particles_user()
+  subroutine inject_particles_user()
     call check(tg_inject(ctx), "inject_particles_user")
   end subroutine
 

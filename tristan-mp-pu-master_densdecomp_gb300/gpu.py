@@ -128,7 +128,11 @@ ENTRY_POINTS = (
 # grid moments of meanq_fld_cur (code/output.F90:5222-5482), by the reference's names
 MOMENTS = ("tdens", "idens", "tbetx", "tbety", "tbetz", "ibetx", "ibety", "ibetz", "tmomx", "tmomy", "tmomz",
            "imomx", "imomy", "imomz", "eener", "iener")
-PHASES = ("fields_pre", "particles", "fields_post", "current", "sort", "diag")
+# tg_phase_times' phases, grouped as the reference's per-lap timers
+# (code/communications.F90:242-326): Field slv = fields_pre + fields_post +
+# add_current, Mover + Deposit = particles, Currnt exch = fold, Filter =
+# filter, Reorder = sort; diag has no counterpart
+PHASES = ("fields_pre", "particles", "fields_post", "fold", "filter", "add_current", "sort", "diag")
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
