@@ -69,6 +69,11 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--sort-every", type=int, default=0, help="0: chosen by the autotuner")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tile", type=int, nargs=3, default=None,
+                    help="tile shape of the single-domain workloads (with --no-autotune)")
+    ap.add_argument("--ppc0", type=float, default=None,
+                    help="particles per cell of both species together (profiling the field kernels on the "
+                         "full grid with few particles)")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-shock", action="store_true")
     ap.add_argument("--shock-steps", type=int, default=100)
@@ -324,6 +329,10 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
     from tristan_gb300 import setups
     device = local
     cfg = setups.make_config(name, diag_every=1, sort_every=max(sort_every, 1))
+    if args.ppc0:
+        cfg.ppc0 = float(args.ppc0)
+    if args.tile and not autotune:
+        cfg.tile = tuple(args.tile)
     ions, lecs = setups.load_beams(cfg, seed=123457 + rank)
     setups.with_capacity(cfg, len(ions), len(lecs))
     n_p = len(ions) + len(lecs)
@@ -343,10 +352,12 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
     ms, phases, kps, clk, hist = run_form(cfg, ions, lecs, warmup, steps, False, device, ws, local, clocks=True)
     ms = allreduce_max(ms, ws, args.impl)
     value = ws * n_p * steps / (ms / 1e3)
-    ms_f, ph_f, _, _, _ = run_form(cfg, ions, lecs, warmup, steps, True, device, ws, local)
-    ms_f = allreduce_max(ms_f, ws, args.impl)
-    fixed = {"value": ws * n_p * steps / (ms_f / 1e3), "ms_per_step": ms_f / steps,
-             "particle_kernel_ms": ph_f["particles"], "deposit": DEPOSIT_FIXED}
+    fixed = None
+    if not args.no_fixed:
+        ms_f, ph_f, _, _, _ = run_form(cfg, ions, lecs, warmup, steps, True, device, ws, local)
+        ms_f = allreduce_max(ms_f, ws, args.impl)
+        fixed = {"value": ws * n_p * steps / (ms_f / 1e3), "ms_per_step": ms_f / steps,
+                 "particle_kernel_ms": ph_f["particles"], "deposit": DEPOSIT_FIXED}
     dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
     ms_e2e = dt_e2e / e2e_steps * 1e3
     ms_link = copy_only_ms(h2d, d2h, device)

@@ -57,6 +57,10 @@ WORKLOADS = {
     # 3D Weibel: 256^3, order 2, 4 ppc/species, gamma0 = 5
     "weibel3d_256_o2": dict(dims=3, order=2, nx=256, ny=256, nz=256, c=0.45, c_omp=8.0,
                             ppc0=8.0, gamma0=5.0, delgam=0.01, ntimes=4),
+    # the same plasma on a 128^3 box (16.8 M particles, 740 MB of particle
+    # data: still above L2) for kernel profiling
+    "weibel3d_128_o2": dict(dims=3, order=2, nx=128, ny=128, nz=128, c=0.45, c_omp=8.0,
+                            ppc0=8.0, gamma0=5.0, delgam=0.01, ntimes=4),
 }
 
 
