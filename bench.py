@@ -366,6 +366,9 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
            "link": {"bound": "host link (NVLink-C2C), both directions at once",
                     "copy_only_ms": ms_link, "achieved_gbs": (h2d + d2h) / ms_e2e / 1e6,
                     "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e},
+           # the lap cannot take less than the longer of its copies and its
+           # device-resident lap (the two overlap part by part)
+           "lap_bound_ms": max(ms_link, ms / steps), "frac_of_lap_bound": max(ms_link, ms / steps) / ms_e2e,
            "mode": "one tg_step_host call per lap: E, B, particle records up; the lap; fields, "
                    "records, counts down (each species in parts: a part is sorted and pushed as soon "
                    "as it is in, and goes home while later parts arrive)",

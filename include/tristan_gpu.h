@@ -457,7 +457,11 @@ int tg_spectrum_x(tg_ctx *ctx, int32_t gambins, float *spec_ions, float *spec_le
    deposit mode, the sort cadence, ntimes and the device; boxes may differ
    in size, shape order, plasma and charges. In fixed-point mode every box
    evolves bit for bit as a single-domain context of the same
-   configuration. Not thread-safe per ensemble.
+   configuration. Not thread-safe per ensemble. An ensemble of up to 72
+   boxes keeps its boxes' tile arguments in a constant-memory table that is
+   one per device and shared by every ensemble of the process: an ensemble
+   stepped after another one on the same device waits for the other's
+   laps first, so the laps of two such ensembles never overlap on the GPU.
    --------------------------------------------------------------------- */
 typedef struct tg_ens tg_ens;
 /* cfgs[0..nbox): one tg_config per box (dims 2, periodic x and y). */

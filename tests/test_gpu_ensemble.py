@@ -161,3 +161,56 @@ def test_ensemble_autotune_and_uneven_sizes():
             np.testing.assert_array_equal(e.fields[b][k], g.fields[k], err_msg=f"box {b} {k}")
         g.close()
     e.close()
+
+
+def test_two_ensembles_share_the_constant_table_in_turn():
+    """Ensembles of up to 72 boxes read their tile arguments from one
+    constant-memory table per device; two ensembles stepped in turn on one
+    device (each waits for the other's laps) stay bit-exact against
+    single-domain contexts"""
+    cfgs_a, parts_a, fields_a = small_ensemble(fixed=1, orders=(3, 1, 2), seed=11)
+    cfgs_b, parts_b, fields_b = small_ensemble(fixed=1, orders=(2, 3), seed=12)
+    ea = build(cfgs_a, parts_a, fields_a)
+    eb = build(cfgs_b, parts_b, fields_b)
+    for _ in range(3):
+        ea.step(2)
+        eb.step(3)
+    ea.sync_to_host()
+    eb.sync_to_host()
+    for cfgs, parts, fields, e, laps in ((cfgs_a, parts_a, fields_a, ea, 6), (cfgs_b, parts_b, fields_b, eb, 9)):
+        for b, c in enumerate(cfgs):
+            g = single(c, *parts[b], fields[b])
+            g.step(laps)
+            g.sync_to_host()
+            for k in ("ex", "bz", "curx", "cury"):
+                np.testing.assert_array_equal(e.fields[b][k], g.fields[k], err_msg=f"box {b} {k}")
+            assert_particles_equal(e.ions(b), g.ions)
+            g.close()
+    ea.close()
+    eb.close()
+
+
+def test_ensemble_beyond_the_constant_table_matches_single_domain():
+    """73 boxes: more than the constant-memory table holds, so the tiles read
+    their arguments from shared memory; still bit-exact per box"""
+    orders = tuple(1 + (b % 3) for b in range(73))
+    cfgs, _ = setups.ensemble_configs(nbox=73, seed=31, sides=(24, 32), ppc_range=(2, 4), fixed=1, sort_every=2)
+    for c, o in zip(cfgs, orders):
+        c.order = o
+        c.c_omp = 4.0
+        c.ntimes = 2
+    parts = setups.load_ensemble(cfgs, seed=7)
+    rng = np.random.default_rng(13)
+    fields = [random_fields(c, rng, scale=0.02) for c in cfgs]
+    e = build(cfgs, parts, fields)
+    e.step(5)
+    e.sync_to_host()
+    for b in (0, 1, 2, 40, 72):
+        g = single(cfgs[b], *parts[b], fields[b])
+        g.step(5)
+        g.sync_to_host()
+        for k in ("ex", "bz", "curx"):
+            np.testing.assert_array_equal(e.fields[b][k], g.fields[k], err_msg=f"box {b} {k}")
+        assert_particles_equal(e.ions(b), g.ions)
+        g.close()
+    e.close()

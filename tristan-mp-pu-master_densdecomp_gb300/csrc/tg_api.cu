@@ -1214,7 +1214,7 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
         CK(mark(ctx, li, 7, 0));
         int rr = run_diag(ctx, true, pipe);
         if (rr) return rr;
-        k += 4 + ctx->g.dims * ctx->cfg.ntimes + (pipe ? pipe->parts - 1 : 0);
+        k += 4 + ctx->cfg.ntimes + (pipe ? pipe->parts - 1 : 0);
         CK(mark(ctx, li, 7, 1));
     }
     *nk = k;

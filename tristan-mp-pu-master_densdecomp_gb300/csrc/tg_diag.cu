@@ -10,13 +10,16 @@
 //                    (gamma-1 = u^2/(gamma+1) in FP32) and momentum summed
 //                    in FP64;
 //  k_rho_to_double   fixed point -> FP64 on the periodic interior;
-//  k_filter64_axis   one FP64 binomial pass on the periodic interior, as
-//                    [1, 2, 1] / 4 along each axis in turn;
-//  k_diag_fields     FP64 reductions: |div E - F(rho)|^2, |F(rho)|^2, total
-//                    charge, field energies and E x B momentum;
+//  k_filter64_pass   one FP64 binomial pass on the periodic interior, as
+//                    [1, 2, 1] / 4 along each axis in turn, all axes of a
+//                    pass in one kernel through a shared-memory tile;
+//  k_diag_fields     FP64 reductions of |div E - F(rho)|^2, |F(rho)|^2 and
+//                    the total charge (div E - F(rho) is a small difference),
+//                    compensated FP32 sums of the field energies and E x B
+//                    momentum;
 //  k_diag_finish     writes the lap's record into the history ring.
 // GB300 has little FP64 throughput, so FP64 is used only where the sums
-// need it (accumulators and the per-cell field reductions).
+// need it (accumulators and the Gauss residual).
 #include <cuda_runtime.h>
 
 #include "tg_particles.cuh"
@@ -117,43 +120,71 @@ __global__ void k_rho_to_double(long long n, double inv, unsigned long long *fx,
     }
 }
 
+static int rgrid(int rows) { return rows < 152 * 16 ? (rows < 1 ? 1 : rows) : 152 * 16; }
+
 // One binomial pass on the periodic interior (nx, ny, nz) is the product of
-// [1, 2, 1] / 4 along each axis; this is the pass along one axis. Weights
-// are powers of two, so every product and partial sum is exact while the
-// values keep below 2^53 units of the fixed-point grid they come from
-// (their order then does not matter). Rows (one y, z) are spread over the
-// blocks, cells of a row over the threads: no 64-bit index divisions.
-template <int AXIS>
-__global__ void __launch_bounds__(256) k_filter64_axis(int nx, int ny, int nz, const double *__restrict__ in,
-                                                       double *__restrict__ out) {
-    const int rows = ny * nz;
-    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
-        const int j = row % ny, k = row / ny;
-        const long long base = (long long)row * nx;
-        long long om = 0, op = 0;  // row offsets of the neighbours (axes 1, 2)
-        if (AXIS == 1) {
-            om = (long long)((j == 0 ? ny - 1 : j - 1) + k * ny) * nx - base;
-            op = (long long)((j == ny - 1 ? 0 : j + 1) + k * ny) * nx - base;
-        } else if (AXIS == 2) {
-            om = (long long)(j + (k == 0 ? nz - 1 : k - 1) * ny) * nx - base;
-            op = (long long)(j + (k == nz - 1 ? 0 : k + 1) * ny) * nx - base;
-        }
-        for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-            const long long t = base + i;
-            double lo, hi;
-            if (AXIS == 0) {
-                lo = in[base + (i == 0 ? nx - 1 : i - 1)];
-                hi = in[base + (i == nx - 1 ? 0 : i + 1)];
-            } else {
-                lo = in[t + om];
-                hi = in[t + op];
-            }
-            out[t] = (2.0 * in[t] + (lo + hi)) * 0.25;
-        }
-    }
+// [1, 2, 1] / 4 along each axis (the current filter's 9 / 27-point weights).
+// A CTA loads its tile with a one-cell halo (periodic images) into shared
+// memory and applies the axis pass (2 c + (l + r)) / 4 along x over the
+// halo rows too, then along y, then z, so the array crosses HBM once per
+// pass. The weights are powers of two: the FP64 products are exact, and the
+// result of each axis step is the same whatever the tiling.
+#define TG_F64_TX 32
+#define TG_F64_TY(DIM) ((DIM) == 3 ? 8 : 16)
+#define TG_F64_TZ(DIM) ((DIM) == 3 ? 8 : 1)
+static size_t filter64_smem(int dims) {
+    const int hx = TG_F64_TX + 2, hy = TG_F64_TY(dims) + 2, hz = dims == 3 ? TG_F64_TZ(dims) + 2 : 1;
+    return (size_t)(hz * hy * hx + hz * hy * TG_F64_TX) * sizeof(double);
 }
 
-static int rgrid(int rows) { return rows < 152 * 16 ? (rows < 1 ? 1 : rows) : 152 * 16; }
+__device__ __forceinline__ int wrap_n(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_filter64_pass(int nx, int ny, int nz, const double *__restrict__ in,
+                                                       double *__restrict__ out) {
+    constexpr int TX = TG_F64_TX, TY = TG_F64_TY(DIM), TZ = TG_F64_TZ(DIM);
+    constexpr int HX = TX + 2, HY = TY + 2, HZ = DIM == 3 ? TZ + 2 : 1;
+    extern __shared__ __align__(16) double f64s[];
+    double *s_in = f64s;                // [HZ][HY][HX]; later the y pass [HZ][TY][TX]
+    double *s_x = f64s + HZ * HY * HX;  // [HZ][HY][TX]
+    const int a0 = blockIdx.x * TX, b0 = blockIdx.y * TY, c0 = blockIdx.z * TZ;
+    for (int t = threadIdx.x; t < HZ * HY * HX; t += blockDim.x) {
+        const int lx = t % HX, r = t / HX, ly = r % HY, lz = r / HY;
+        const int a = wrap_n(a0 - 1 + lx, nx), b = wrap_n(b0 - 1 + ly, ny);
+        const int c = DIM == 3 ? wrap_n(c0 - 1 + lz, nz) : 0;
+        s_in[t] = in[((long long)c * ny + b) * nx + a];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < HZ * HY * TX; t += blockDim.x) {
+        const int lx = t % TX, row = t / TX;
+        const double *p = s_in + row * HX + lx;
+        s_x[t] = (2.0 * p[1] + (p[0] + p[2])) * 0.25;
+    }
+    __syncthreads();
+    double *s_y = s_in;  // [HZ][TY][TX]
+    for (int t = threadIdx.x; t < HZ * TY * TX; t += blockDim.x) {
+        const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
+        const double *p = s_x + (lz * HY + ly) * TX + lx;
+        s_y[t] = (2.0 * p[TX] + (p[0] + p[2 * TX])) * 0.25;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < TZ * TY * TX; t += blockDim.x) {
+        const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
+        const int a = a0 + lx, b = b0 + ly, c = c0 + lz;
+        if (a >= nx || b >= ny || c >= nz) continue;
+        double v;
+        if (DIM == 3) {
+            const double *p = s_y + (lz * TY + ly) * TX + lx;
+            v = (2.0 * p[TY * TX] + (p[0] + p[2 * TY * TX])) * 0.25;
+        } else {
+            v = s_y[ly * TX + lx];
+        }
+        out[((long long)c * ny + b) * nx + a] = v;
+    }
+}
 
 template <int DIM>
 __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__restrict__ ex, const float *__restrict__ ey,
@@ -162,7 +193,11 @@ __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__rest
                                                      const double *__restrict__ rho, double *acc) {
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
     const int lo = g.ng / 2 + 1, loz = DIM == 3 ? g.ngz / 2 + 1 : 1;
-    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // res2 rho2 charge eE eB fx fy fz
+    double v[3] = {0, 0, 0};  // res2 rho2 charge: FP64 (the residual is a small difference)
+    // field energies and momentum eE eB fx fy fz: per-thread compensated FP32
+    // sums, one FP64 conversion per thread (GB300 issues FP64 at a small
+    // fraction of the FP32 rate)
+    float ks[5] = {0, 0, 0, 0, 0}, kc[5] = {0, 0, 0, 0, 0};
     // rows (one y, z) over the blocks, cells of a row over the threads
     for (int row = blockIdx.x; row < ny * nz; row += gridDim.x)
     for (int a = threadIdx.x; a < nx; a += blockDim.x) {
@@ -181,17 +216,21 @@ __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__rest
         v[0] += res * res;
         v[1] += rh * rh;
         v[2] += rh;
-        const double e0 = ex[l], e1 = ey[l], e2 = ez[l], b0 = bx[l], b1 = by[l], b2 = bz[l];
-        v[3] += 0.5 * (e0 * e0 + e1 * e1 + e2 * e2);
-        v[4] += 0.5 * (b0 * b0 + b1 * b1 + b2 * b2);
-        v[5] += e1 * b2 - e2 * b1;
-        v[6] += e2 * b0 - e0 * b2;
-        v[7] += e0 * b1 - e1 * b0;
+        const float e0 = ex[l], e1 = ey[l], e2 = ez[l], b0 = bx[l], b1 = by[l], b2 = bz[l];
+        const float terms[5] = {0.5f * (e0 * e0 + e1 * e1 + e2 * e2), 0.5f * (b0 * b0 + b1 * b1 + b2 * b2),
+                                e1 * b2 - e2 * b1, e2 * b0 - e0 * b2, e0 * b1 - e1 * b0};
+#pragma unroll
+        for (int q = 0; q < 5; q++) {  // Kahan summation
+            const float y = terms[q] - kc[q];
+            const float t2 = ks[q] + y;
+            kc[q] = (t2 - ks[q]) - y;
+            ks[q] = t2;
+        }
     }
-    double first[5] = {v[0], v[1], v[2], v[3], v[4]};
+    double first[5] = {v[0], v[1], v[2], (double)ks[0] - (double)kc[0], (double)ks[1] - (double)kc[1]};
     block_accumulate<5>(first, acc, D_RES2);
     __syncthreads();
-    double second[3] = {v[5], v[6], v[7]};
+    double second[3] = {(double)ks[2] - (double)kc[2], (double)ks[3] - (double)kc[3], (double)ks[4] - (double)kc[4]};
     block_accumulate<3>(second, acc, D_FX);
 }
 
@@ -663,15 +702,17 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
     k_rho_to_double<<<dgrid(n), 256, 0, st>>>(n, d.P.fx_inv, d.rhofx, d.rho[0]);
     double *cur = d.rho[0], *nxt = d.rho[1];
     const int rg = rgrid(ny * nz);
+    const size_t fsm = filter64_smem(g.dims);
+    const dim3 fgrid((nx + TG_F64_TX - 1) / TG_F64_TX, (ny + TG_F64_TY(g.dims) - 1) / TG_F64_TY(g.dims),
+                     (nz + TG_F64_TZ(g.dims) - 1) / TG_F64_TZ(g.dims));
+    if (g.dims == 3) e = cudaFuncSetAttribute(k_filter64_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+    if (e != cudaSuccess) return e;
     for (int p = 0; p < d.ntimes; p++) {
-        for (int ax = 0; ax < g.dims; ax++) {
-            if (ax == 0) k_filter64_axis<0><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
-            else if (ax == 1) k_filter64_axis<1><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
-            else k_filter64_axis<2><<<rg, 256, 0, st>>>(nx, ny, nz, cur, nxt);
-            double *t = cur;
-            cur = nxt;
-            nxt = t;
-        }
+        if (g.dims == 3) k_filter64_pass<3><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
+        else k_filter64_pass<2><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
+        double *t = cur;
+        cur = nxt;
+        nxt = t;
     }
     if (g.dims == 3)
         k_diag_fields<3><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);

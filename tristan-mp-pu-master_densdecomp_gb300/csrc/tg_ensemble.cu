@@ -21,6 +21,8 @@
 // 117-303) steps.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -156,37 +158,73 @@ __global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
     }
 }
 
-// tile counting sort over all boxes: grid.y = box
-__global__ void k_ens_count(const Geom *__restrict__ geoms, Species sp, const long long *__restrict__ bstart,
+// The same kernel reading its box's arguments from a constant-memory table
+// (the arguments are uniform across the CTA, so every read is a broadcast
+// from the constant cache). With the arguments in shared memory the deposit
+// loop re-reads them there and the kernel ran 1.2x slower per particle than
+// the single-domain one. The table holds up to TG_ENS_CONST_BOXES boxes; it
+// is one per device, shared by every ensemble of the process (see
+// claim_const_table); larger ensembles use k_ens_tiles.
+#define TG_ENS_CONST_BOXES 72
+__constant__ TileArgs c_ens_targs[TG_ENS_CONST_BOXES];
+template <int ORDER, bool FIXED>
+__global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
+    k_ens_tiles_c(const int2 *__restrict__ work, int nwork, int *queue) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int wi = s_item;
+        if (wi >= nwork) break;  // uniform across the CTA
+        const int2 it = work[wi];
+        tile_body<2, ORDER, FIXED, true, true>(c_ens_targs[it.x], it.y, smem_raw);
+        __syncthreads();  // window free for the next tile
+    }
+}
+
+// tile counting sort over all boxes: one flat grid over the particles of
+// every box (stored box after box), so a large box gets as many threads as
+// its particles need; a particle's box is found by bisection of the box
+// starts (the last box whose start is at or before it: empty boxes skipped)
+__device__ __forceinline__ int ens_box_of(const long long *__restrict__ bstart, int nbox, long long n) {
+    int lo = 0, hi = nbox;  // bstart[lo] <= n < bstart[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(bstart + mid) <= n) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_ens_count(const Geom *__restrict__ geoms, Species sp, const long long *__restrict__ bstart, int nbox,
                             const int *__restrict__ tofs, int *hist) {
-    const int b = blockIdx.y;
-    const Geom &g = geoms[b];
-    const long long n1 = bstart[b + 1];
-    const int t0 = tofs[b];
-    for (long long n = bstart[b] + blockIdx.x * (long long)blockDim.x + threadIdx.x; n < n1;
+    const long long total = bstart[nbox];
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
         const int cell = sp.cell[n];
         if (cell < 0) continue;
+        const int b = ens_box_of(bstart, nbox, n);
+        const Geom &g = geoms[b];
         int i, j, k;
         cell_ijk(g, cell, i, j, k);
-        agg_inc(hist, t0 + tile_of(g, i, j, k));
+        agg_inc(hist, tofs[b] + tile_of(g, i, j, k));
     }
 }
 
 __global__ void k_ens_scatter(const Geom *__restrict__ geoms, Species src, Species dst,
-                              const long long *__restrict__ bstart, const int *__restrict__ tofs, const int *start,
-                              int *cursor) {
-    const int b = blockIdx.y;
-    const Geom &g = geoms[b];
-    const long long n1 = bstart[b + 1];
-    const int t0 = tofs[b];
-    for (long long n = bstart[b] + blockIdx.x * (long long)blockDim.x + threadIdx.x; n < n1;
+                              const long long *__restrict__ bstart, int nbox, const int *__restrict__ tofs,
+                              const int *start, int *cursor) {
+    const long long total = bstart[nbox];
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < total;
          n += (long long)gridDim.x * blockDim.x) {
         const int cell = src.cell[n];
         if (cell < 0) continue;
+        const int b = ens_box_of(bstart, nbox, n);
+        const Geom &g = geoms[b];
         int i, j, k;
         cell_ijk(g, cell, i, j, k);
-        const int t = t0 + tile_of(g, i, j, k);
+        const int t = tofs[b] + tile_of(g, i, j, k);
         const long long d = (long long)start[t] + agg_inc(cursor, t);
         dst.cell[d] = cell;
         dst.ox[d] = src.ox[n];
@@ -227,6 +265,8 @@ struct tg_ens {
     int sort_every = 1, ntimes = 4;
     size_t smem = 0;
     int tile_grid[3] = {0, 0, 0};  // per shape order
+    bool use_const = false;        // tile arguments from the constant-memory table
+    cudaEvent_t laps_done = nullptr;  // after the last tg_ens_step's laps
     cudaStream_t st = nullptr;
     int device = 0;
     float *f[9] = {};
@@ -273,6 +313,15 @@ struct tg_ens {
 };
 
 static thread_local char g_ens_error[512];
+
+// The constant-memory table of tile arguments is one per device and shared
+// by every ensemble of the process: each lap copies its boxes' arguments
+// into it before its tile kernels. An ensemble that steps after another
+// one on the same device first makes its stream wait for the other's last
+// laps (an event), so their laps never overlap on the table.
+#define TG_ENS_MAX_DEVICES 64
+static std::mutex g_const_mu;
+static tg_ens *g_const_owner[TG_ENS_MAX_DEVICES] = {};
 
 static int efail(tg_ens *E, int code, const char *fmt, ...) {
     char buf[512];
@@ -563,6 +612,20 @@ extern "C" int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out) {
             if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kerns[o], 256, E->smem);
             E->tile_grid[o] = nsm * per_sm;
         }
+        void (*kc[3])(const int2 *, int, int *);
+        if (E->fixed) {
+            kc[0] = k_ens_tiles_c<1, true>;
+            kc[1] = k_ens_tiles_c<2, true>;
+            kc[2] = k_ens_tiles_c<3, true>;
+        } else {
+            kc[0] = k_ens_tiles_c<1, false>;
+            kc[1] = k_ens_tiles_c<2, false>;
+            kc[2] = k_ens_tiles_c<3, false>;
+        }
+        for (int o = 0; o < 3 && e == cudaSuccess; o++)
+            e = cudaFuncSetAttribute(kc[o], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem);
+        E->use_const = E->nbox <= TG_ENS_CONST_BOXES && E->device >= 0 && E->device < TG_ENS_MAX_DEVICES;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->laps_done, cudaEventDisableTiming);
         for (int b = 0; b < 2 && e == cudaSuccess; b++) {
             e = cudaStreamCreateWithFlags(&E->side[b], cudaStreamNonBlocking);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->join[b], cudaEventDisableTiming);
@@ -611,6 +674,12 @@ extern "C" void tg_ens_finalize(tg_ens *E) {
     if (!E) return;
     cudaSetDevice(E->device);
     if (E->st) cudaStreamSynchronize(E->st);
+    {
+        std::lock_guard<std::mutex> lock(g_const_mu);
+        if (E->device >= 0 && E->device < TG_ENS_MAX_DEVICES && g_const_owner[E->device] == E)
+            g_const_owner[E->device] = nullptr;
+    }
+    if (E->laps_done) cudaEventDestroy(E->laps_done);
     for (int p = 0; p < 2; p++)
         if (E->cycle[p]) cudaGraphExecDestroy(E->cycle[p]);
     for (void *q : E->allocs) cudaFree(q);
@@ -678,15 +747,19 @@ static int build_work(tg_ens *E, const std::vector<long long> &nb) {
 
 static int sort_species(tg_ens *E, int s, bool counted) {
     const int p = E->par;
-    const dim3 grid(64, E->nbox);
+    // a flat grid over the particles of every box
+    const long long per = E->capacity / 256 + 1;
+    const int grid = (int)(per < 152 * 16 ? per : 152 * 16);
     if (!counted) {
-        k_ens_count<<<grid, 256, 0, E->st>>>(E->d_geom, E->sp[p][s], E->bstart[p][s], E->d_tofs, E->hist[s]);
+        k_ens_count<<<grid, 256, 0, E->st>>>(E->d_geom, E->sp[p][s], E->bstart[p][s], E->nbox, E->d_tofs,
+                                             E->hist[s]);
         ECK(cudaGetLastError());
     }
     ECK(launch_scan(E->hist[s], E->tstart[s], E->cursor[s], E->T, E->d_cnt + 2 * (1 - p) + s, E->st));
     k_ens_bstart<<<1, 256, 0, E->st>>>(E->d_tofs, E->tstart[s], E->bstart[1 - p][s], E->nbox);
     ECK(cudaGetLastError());
-    k_ens_scatter<<<grid, 256, 0, E->st>>>(E->d_geom, E->sp[p][s], E->sp[1 - p][s], E->bstart[p][s], E->d_tofs,
+    k_ens_scatter<<<grid, 256, 0, E->st>>>(E->d_geom, E->sp[p][s], E->sp[1 - p][s], E->bstart[p][s], E->nbox,
+                                           E->d_tofs,
                                            E->tstart[s], E->cursor[s]);
     ECK(cudaGetLastError());
     return TG_OK;
@@ -855,6 +928,10 @@ static int ens_lap(tg_ens *E, bool sort_now, int *nk) {
     const TileArgs *ta = E->d_targs + (size_t)(E->par * 2 + (sort_now ? 1 : 0)) * E->nbox;
     // shape order 3 on the lap's stream, orders 2 and 1 on two branches that
     // fill the SMs as the order-3 tiles drain
+    // this lap's tile arguments into the constant-memory table
+    if (E->use_const)
+        ECK(cudaMemcpyToSymbolAsync(c_ens_targs, ta, (size_t)E->nbox * sizeof(TileArgs), 0, cudaMemcpyDeviceToDevice,
+                                    st));
     ECK(cudaEventRecord(E->fork, st));
     for (int b = 0; b < 2; b++) ECK(cudaStreamWaitEvent(E->side[b], E->fork, 0));
     for (int o = 3; o >= 1; o--) {
@@ -863,6 +940,20 @@ static int ens_lap(tg_ens *E, bool sort_now, int *nk) {
         const int nw = E->nwork[o - 1];
         int *qu = E->queue + (o - 1);
         const int grid = E->tile_grid[o - 1];
+        if (nw > 0 && E->use_const) {
+            if (E->fixed) {
+                if (o == 3) k_ens_tiles_c<3, true><<<grid, 256, E->smem, so>>>(w, nw, qu);
+                else if (o == 2) k_ens_tiles_c<2, true><<<grid, 256, E->smem, so>>>(w, nw, qu);
+                else k_ens_tiles_c<1, true><<<grid, 256, E->smem, so>>>(w, nw, qu);
+            } else {
+                if (o == 3) k_ens_tiles_c<3, false><<<grid, 256, E->smem, so>>>(w, nw, qu);
+                else if (o == 2) k_ens_tiles_c<2, false><<<grid, 256, E->smem, so>>>(w, nw, qu);
+                else k_ens_tiles_c<1, false><<<grid, 256, E->smem, so>>>(w, nw, qu);
+            }
+            ECK(cudaGetLastError());
+            k++;
+            continue;
+        }
         if (nw > 0) {
             if (E->fixed) {
                 if (o == 3) k_ens_tiles<3, true><<<grid, 256, E->smem, so>>>(ta, w, nw, qu);
@@ -947,10 +1038,32 @@ static int capture_cycle(tg_ens *E, int start_par) {
     return TG_OK;
 }
 
+// called with g_const_mu held
+static int claim_const_table(tg_ens *E) {
+    tg_ens *&owner = g_const_owner[E->device];
+    if (owner && owner != E) ECK(cudaStreamWaitEvent(E->st, owner->laps_done, 0));
+    owner = E;
+    return TG_OK;
+}
+
+static int ens_step_laps(tg_ens *E, int32_t nsteps);
+
 extern "C" int tg_ens_step(tg_ens *E, int32_t nsteps) {
     if (!E || nsteps < 0) return TG_ERR_ARG;
     int r = ensure_sorted(E);
     if (r) return r;
+    if (!E->use_const) return ens_step_laps(E, nsteps);
+    // the laps are issued under the table's lock, so another ensemble that
+    // steps next on this device waits for exactly these laps
+    std::lock_guard<std::mutex> lock(g_const_mu);
+    if ((r = claim_const_table(E))) return r;
+    if ((r = ens_step_laps(E, nsteps))) return r;
+    ECK(cudaEventRecord(E->laps_done, E->st));
+    return TG_OK;
+}
+
+static int ens_step_laps(tg_ens *E, int32_t nsteps) {
+    int r = TG_OK;
     if (nsteps > 0) E->may_have_dead = true;
     const int se = E->sort_every, cyc = 2 * se;
     int left = nsteps;

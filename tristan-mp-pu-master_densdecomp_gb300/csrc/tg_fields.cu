@@ -173,43 +173,76 @@ __global__ void __launch_bounds__(256) k_filter(Geom g, const float *__restrict_
 // cells and marches up TG_F3_KC planes, keeping the refreshed input planes
 // k-1, k, k+1 (with a one-cell halo) of all three components in a ring, so
 // every input element is read from HBM about once per pass instead of 27
-// times through the cache. Each cell then runs the same selection and the
-// same stencil27 as filter_one.
+// times through the cache. The plane k+2 is loaded into registers before
+// plane k is filtered and stored into the ring after it, so its memory
+// latency overlaps the stencil work. Each cell then runs the same selection
+// and the same stencil27 as filter_one.
 #define TG_F3_TX 32
 #define TG_F3_TY 8
-#define TG_F3_KC 16
+#define TG_F3_KC 32
+#define TG_F3_SX (TG_F3_TX + 2)
+#define TG_F3_SY (TG_F3_TY + 2)
+#define TG_F3_PER ((TG_F3_SX * TG_F3_SY + TG_F3_TX * TG_F3_TY - 1) / (TG_F3_TX * TG_F3_TY))  // halo cells per thread
 __global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
     k_filter3d(Geom g, const float *__restrict__ i0, const float *__restrict__ i1, const float *__restrict__ i2,
                float *o0, float *o1, float *o2) {
-    constexpr int SX = TG_F3_TX + 2, SY = TG_F3_TY + 2;
+    constexpr int SX = TG_F3_SX, SY = TG_F3_SY, PER = TG_F3_PER;
     __shared__ float sm[3][3][SY][SX];  // [component][plane ring][y][x]
     const RefreshMap Rx{g.mx, g.ng, g.per[0]}, Ry{g.my, g.ng, g.per[1]}, Rz{g.mz, g.ngz, g.per[2]};
     const int ib = blockIdx.x * TG_F3_TX + 1, jb = blockIdx.y * TG_F3_TY + 1;
     const int kb = blockIdx.z * TG_F3_KC + 1;
     const int ke = min(kb + TG_F3_KC, g.mz + 1);
     const int tid = threadIdx.y * TG_F3_TX + threadIdx.x;
-    const float *in[3] = {i0, i1, i2};
-    auto load_plane = [&](int k) {
-        const int slot = (k + 3) % 3;
-        for (int t = tid; t < SX * SY; t += TG_F3_TX * TG_F3_TY) {
-            const int lx = t % SX, ly = t / SX;
-            const int i = ib - 1 + lx, j = jb - 1 + ly;
-            const bool ok = i >= 1 && i <= g.mx && j >= 1 && j <= g.my && k >= 1 && k <= g.mz;
-            const long long l = ok ? lin(g, Rx(i), Ry(j), Rz(k)) : 0;
+    // this thread's halo cells of a plane: their (refreshed) x-y offset, or
+    // -1 outside the array; each plane adds its (refreshed) z offset
+    long long xy[PER];
+    int slot_xy[PER];
 #pragma unroll
-            for (int c = 0; c < 3; c++) sm[c][slot][ly][lx] = ok ? in[c][l] : 0.0f;
+    for (int e = 0; e < PER; e++) {
+        const int t = tid + e * TG_F3_TX * TG_F3_TY;
+        slot_xy[e] = t < SX * SY ? t : -1;
+        xy[e] = -1;
+        if (t < SX * SY) {
+            const int i = ib - 1 + t % SX, j = jb - 1 + t / SX;
+            if (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) xy[e] = lin(g, Rx(i), Ry(j), 1);
         }
+    }
+    float stage[3][PER];
+    auto fetch = [&](int k) {  // plane k into registers
+        const bool kin = k >= 1 && k <= g.mz;
+        const long long zo = kin ? g.sz * (long long)(Rz(k) - 1) : 0;
+#pragma unroll
+        for (int e = 0; e < PER; e++) {
+            const bool ok = kin && xy[e] >= 0;
+            stage[0][e] = ok ? i0[xy[e] + zo] : 0.0f;
+            stage[1][e] = ok ? i1[xy[e] + zo] : 0.0f;
+            stage[2][e] = ok ? i2[xy[e] + zo] : 0.0f;
+        }
+    };
+    auto put = [&](int k) {  // registers into plane k's ring slot
+        const int slot = (k + 3) % 3;
+#pragma unroll
+        for (int e = 0; e < PER; e++)
+            if (slot_xy[e] >= 0) {
+                const int lx = slot_xy[e] % SX, ly = slot_xy[e] / SX;
+#pragma unroll
+                for (int c = 0; c < 3; c++) sm[c][slot][ly][lx] = stage[c][e];
+            }
     };
     const int ilo = g.ng / 2 + 1, ihi = g.mx - (g.ng / 2 + 1);
     const int jlo = g.ng / 2 + 1, jhi = g.my - (g.ng / 2 + 1);
     const int klo = g.ngz / 2 + 1, khi = g.mz - (g.ngz / 2 + 1);
     const int i = ib + threadIdx.x, j = jb + threadIdx.y;
     const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
-    load_plane(kb - 1);
-    load_plane(kb);
+    fetch(kb - 1);
+    put(kb - 1);
+    fetch(kb);
+    put(kb);
+    fetch(kb + 1);
+    put(kb + 1);
+    __syncthreads();
     for (int k = kb; k < ke; k++) {
-        load_plane(k + 1);
-        __syncthreads();
+        if (k + 1 < ke) fetch(k + 2);  // in flight while plane k is filtered
         if (i <= g.mx && j <= g.my) {
             const bool in_ik = i >= ilo && i <= ihi && k >= klo && k <= khi;
             const bool in_xy = in_ik && j >= jlo && j <= jhi;
@@ -233,7 +266,11 @@ __global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
             o1[t] = res[1];
             o2[t] = res[2];
         }
-        __syncthreads();
+        __syncthreads();  // plane k-1's slot is free
+        if (k + 1 < ke) {
+            put(k + 2);
+            __syncthreads();
+        }
     }
 }
 
