@@ -149,6 +149,8 @@ static int check_status(tg_ctx *ctx) {
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->st));
     if (st & ST_NAN) return fail(ctx, TG_ERR_NAN, "non-finite particle coordinate (device status %d)", st);
     if (st & ST_OVERFLOW) return fail(ctx, TG_ERR_OVERFLOW, "particle capacity exceeded (device status %d)", st);
+    if (st & ST_CHARGE_GRID)
+        return fail(ctx, TG_ERR_OVERFLOW, "diagnostics: a node holds 2^17 particle charges or more (device status %d)", st);
     return fail(ctx, TG_ERR_BOUNDS, "particle or deposit outside the local grid (device status %d)", st);
 }
 

@@ -9,10 +9,11 @@
 //                    so the sum is order independent), kinetic energy
 //                    (gamma-1 = u^2/(gamma+1) in FP32) and momentum summed
 //                    in FP64;
-//  k_rho_to_double   fixed point -> FP64 on the periodic interior;
-//  k_filter64_pass   one FP64 binomial pass on the periodic interior, as
-//                    [1, 2, 1] / 4 along each axis in turn, all axes of a
-//                    pass in one kernel through a shared-memory tile;
+//  k_rho_to_int      fixed point -> the filter's finer integer grid;
+//  k_filter_rho_pass one binomial pass on the periodic interior, as
+//                    [1, 2, 1] / 4 along each axis in turn in int64 (each
+//                    step rounded to the grid), all axes of a pass in one
+//                    kernel through a shared-memory tile;
 //  k_diag_fields     FP64 reductions of |div E - F(rho)|^2, |F(rho)|^2 and
 //                    the total charge (div E - F(rho) is a small difference),
 //                    compensated FP32 sums of the field energies and E x B
@@ -112,10 +113,18 @@ __global__ void __launch_bounds__(256, TG_DIAG_MINB) k_diag_particles(DiagArgs a
     block_accumulate<5>(part, a.acc, D_EKI);
 }
 
-__global__ void k_rho_to_double(long long n, double inv, unsigned long long *fx, double *rho) {
+// fixed point -> the filter's integer grid: 16 more fraction bits, so the
+// rounding of the filter's divisions stays far below the Gauss residual; a
+// sum of 2^47 units or more (2^17 full particle charges on one node) would
+// overflow the filter and is flagged. The accumulator is cleared for the
+// next lap.
+#define TG_RHO_SHIFT 16
+__global__ void k_rho_to_int(long long n, unsigned long long *fx, long long *rho, int *status) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
-        rho[t] = __ll2double_rn((long long)fx[t]) * inv;
+        const long long v = (long long)fx[t];
+        if (v >= (1LL << 47) || v <= -(1LL << 47)) atomicOr(status, ST_CHARGE_GRID);
+        rho[t] = (long long)((unsigned long long)v << TG_RHO_SHIFT);
         fx[t] = 0ull;
     }
 }
@@ -123,18 +132,19 @@ __global__ void k_rho_to_double(long long n, double inv, unsigned long long *fx,
 static int rgrid(int rows) { return rows < 152 * 16 ? (rows < 1 ? 1 : rows) : 152 * 16; }
 
 // One binomial pass on the periodic interior (nx, ny, nz) is the product of
-// [1, 2, 1] / 4 along each axis (the current filter's 9 / 27-point weights).
-// A CTA loads its tile with a one-cell halo (periodic images) into shared
-// memory and applies the axis pass (2 c + (l + r)) / 4 along x over the
-// halo rows too, then along y, then z, so the array crosses HBM once per
-// pass. The weights are powers of two: the FP64 products are exact, and the
-// result of each axis step is the same whatever the tiling.
+// [1, 2, 1] / 4 along each axis (the current filter's 9 / 27-point weights),
+// applied here to the charge on its integer grid: each axis step is
+// (l + 2 c + r + 2) >> 2 in int64, rounded to the grid (2^-(fx_shift + 16)
+// of the fixed-point unit), integer work where FP64 would set the pace on
+// this GPU. A CTA loads its tile with a one-cell halo (periodic images) into
+// shared memory and steps along x over the halo rows too, then along y, then
+// z, so the array crosses HBM once per pass.
 #define TG_F64_TX 32
 #define TG_F64_TY(DIM) ((DIM) == 3 ? 8 : 16)
 #define TG_F64_TZ(DIM) ((DIM) == 3 ? 8 : 1)
 static size_t filter64_smem(int dims) {
     const int hx = TG_F64_TX + 2, hy = TG_F64_TY(dims) + 2, hz = dims == 3 ? TG_F64_TZ(dims) + 2 : 1;
-    return (size_t)(hz * hy * hx + hz * hy * TG_F64_TX) * sizeof(double);
+    return (size_t)(hz * hy * hx + hz * hy * TG_F64_TX) * sizeof(long long);
 }
 
 __device__ __forceinline__ int wrap_n(int i, int n) {
@@ -142,14 +152,18 @@ __device__ __forceinline__ int wrap_n(int i, int n) {
     return i < 0 ? i + n : i;
 }
 
+__device__ __forceinline__ long long binom_step(long long l, long long c, long long r) {
+    return (l + 2 * c + r + 2) >> 2;
+}
+
 template <int DIM>
-__global__ void __launch_bounds__(256) k_filter64_pass(int nx, int ny, int nz, const double *__restrict__ in,
-                                                       double *__restrict__ out) {
+__global__ void __launch_bounds__(256) k_filter_rho_pass(int nx, int ny, int nz, const long long *__restrict__ in,
+                                                         long long *__restrict__ out) {
     constexpr int TX = TG_F64_TX, TY = TG_F64_TY(DIM), TZ = TG_F64_TZ(DIM);
     constexpr int HX = TX + 2, HY = TY + 2, HZ = DIM == 3 ? TZ + 2 : 1;
-    extern __shared__ __align__(16) double f64s[];
-    double *s_in = f64s;                // [HZ][HY][HX]; later the y pass [HZ][TY][TX]
-    double *s_x = f64s + HZ * HY * HX;  // [HZ][HY][TX]
+    extern __shared__ __align__(16) long long rhos[];
+    long long *s_in = rhos;                // [HZ][HY][HX]; later the y step [HZ][TY][TX]
+    long long *s_x = rhos + HZ * HY * HX;  // [HZ][HY][TX]
     const int a0 = blockIdx.x * TX, b0 = blockIdx.y * TY, c0 = blockIdx.z * TZ;
     for (int t = threadIdx.x; t < HZ * HY * HX; t += blockDim.x) {
         const int lx = t % HX, r = t / HX, ly = r % HY, lz = r / HY;
@@ -160,25 +174,25 @@ __global__ void __launch_bounds__(256) k_filter64_pass(int nx, int ny, int nz, c
     __syncthreads();
     for (int t = threadIdx.x; t < HZ * HY * TX; t += blockDim.x) {
         const int lx = t % TX, row = t / TX;
-        const double *p = s_in + row * HX + lx;
-        s_x[t] = (2.0 * p[1] + (p[0] + p[2])) * 0.25;
+        const long long *p = s_in + row * HX + lx;
+        s_x[t] = binom_step(p[0], p[1], p[2]);
     }
     __syncthreads();
-    double *s_y = s_in;  // [HZ][TY][TX]
+    long long *s_y = s_in;  // [HZ][TY][TX]
     for (int t = threadIdx.x; t < HZ * TY * TX; t += blockDim.x) {
         const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
-        const double *p = s_x + (lz * HY + ly) * TX + lx;
-        s_y[t] = (2.0 * p[TX] + (p[0] + p[2 * TX])) * 0.25;
+        const long long *p = s_x + (lz * HY + ly) * TX + lx;
+        s_y[t] = binom_step(p[0], p[TX], p[2 * TX]);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < TZ * TY * TX; t += blockDim.x) {
         const int lx = t % TX, r = t / TX, ly = r % TY, lz = r / TY;
         const int a = a0 + lx, b = b0 + ly, c = c0 + lz;
         if (a >= nx || b >= ny || c >= nz) continue;
-        double v;
+        long long v;
         if (DIM == 3) {
-            const double *p = s_y + (lz * TY + ly) * TX + lx;
-            v = (2.0 * p[TY * TX] + (p[0] + p[2 * TY * TX])) * 0.25;
+            const long long *p = s_y + (lz * TY + ly) * TX + lx;
+            v = binom_step(p[0], p[TY * TX], p[2 * TY * TX]);
         } else {
             v = s_y[ly * TX + lx];
         }
@@ -190,7 +204,7 @@ template <int DIM>
 __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__restrict__ ex, const float *__restrict__ ey,
                                                      const float *__restrict__ ez, const float *__restrict__ bx,
                                                      const float *__restrict__ by, const float *__restrict__ bz,
-                                                     const double *__restrict__ rho, double *acc) {
+                                                     const long long *__restrict__ rho, double inv, double *acc) {
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = DIM == 3 ? g.mz - g.ngz : 1;
     const int lo = g.ng / 2 + 1, loz = DIM == 3 ? g.ngz / 2 + 1 : 1;
     double v[3] = {0, 0, 0};  // res2 rho2 charge: FP64 (the residual is a small difference)
@@ -211,7 +225,7 @@ __global__ void __launch_bounds__(256) k_diag_fields(Geom g, const float *__rest
             const int km = c == 0 ? loz + nz - 1 : k - 1;
             div += (double)ez[l] - (double)ez[lin(g, i, j, km)];
         }
-        const double rh = rho[t];
+        const double rh = __ll2double_rn(rho[t]) * inv;
         const double res = div - rh;
         v[0] += res * res;
         v[1] += rh * rh;
@@ -699,25 +713,28 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = g.dims == 3 ? g.mz - g.ngz : 1;
     const long long n = (long long)nx * ny * nz;
-    k_rho_to_double<<<dgrid(n), 256, 0, st>>>(n, d.P.fx_inv, d.rhofx, d.rho[0]);
-    double *cur = d.rho[0], *nxt = d.rho[1];
+    // the two FP64 scratch arrays hold the charge on its integer grid
+    long long *cur = reinterpret_cast<long long *>(d.rho[0]), *nxt = reinterpret_cast<long long *>(d.rho[1]);
+    k_rho_to_int<<<dgrid(n), 256, 0, st>>>(n, d.rhofx, cur, d.status);
     const int rg = rgrid(ny * nz);
     const size_t fsm = filter64_smem(g.dims);
     const dim3 fgrid((nx + TG_F64_TX - 1) / TG_F64_TX, (ny + TG_F64_TY(g.dims) - 1) / TG_F64_TY(g.dims),
                      (nz + TG_F64_TZ(g.dims) - 1) / TG_F64_TZ(g.dims));
-    if (g.dims == 3) e = cudaFuncSetAttribute(k_filter64_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+    if (g.dims == 3)
+        e = cudaFuncSetAttribute(k_filter_rho_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
     if (e != cudaSuccess) return e;
     for (int p = 0; p < d.ntimes; p++) {
-        if (g.dims == 3) k_filter64_pass<3><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
-        else k_filter64_pass<2><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
-        double *t = cur;
+        if (g.dims == 3) k_filter_rho_pass<3><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
+        else k_filter_rho_pass<2><<<fgrid, 256, fsm, st>>>(nx, ny, nz, cur, nxt);
+        long long *t = cur;
         cur = nxt;
         nxt = t;
     }
+    const double inv = d.P.fx_inv / (double)(1LL << TG_RHO_SHIFT);
     if (g.dims == 3)
-        k_diag_fields<3><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+        k_diag_fields<3><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, inv, d.acc);
     else
-        k_diag_fields<2><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, d.acc);
+        k_diag_fields<2><<<rg, 256, 0, st>>>(g, d.f[0], d.f[1], d.f[2], d.f[3], d.f[4], d.f[5], cur, inv, d.acc);
     k_diag_finish<<<1, 32, 0, st>>>(d.acc, d.hist, d.hist_cap, d.counter);
     return cudaGetLastError();
 }

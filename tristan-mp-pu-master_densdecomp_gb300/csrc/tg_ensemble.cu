@@ -390,6 +390,8 @@ static int check_status(tg_ens *E) {
     ECK(cudaMemsetAsync(E->d_status, 0, sizeof(int), E->st));
     if (st & ST_NAN) return efail(E, TG_ERR_NAN, "non-finite particle coordinate (device status %d)", st);
     if (st & ST_OVERFLOW) return efail(E, TG_ERR_OVERFLOW, "particle capacity exceeded (device status %d)", st);
+    if (st & ST_CHARGE_GRID)
+        return efail(E, TG_ERR_OVERFLOW, "diagnostics: a node holds 2^17 particle charges or more (device status %d)", st);
     return efail(E, TG_ERR_BOUNDS, "particle or deposit outside its box (device status %d)", st);
 }
 

@@ -295,10 +295,11 @@ __global__ void k_primal(Geom g, const float *__restrict__ ex, const float *__re
                          float *pbz) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.lot;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.mx) + 1;
-        const long long r = t / g.mx;
-        const int j = (int)(r % g.my) + 1;
-        const int k = (int)(r / g.my) + 1;
+        const int ti = (int)t;  // fewer than 2^31 cells
+        const int i = ti % g.mx + 1;
+        const int r = ti / g.mx;
+        const int j = r % g.my + 1;
+        const int k = r / g.my + 1;
         const int im = i == 1 ? g.mx : i - 1, jm = j == 1 ? g.my : j - 1, km = k == 1 ? g.mz : k - 1;
         const long long lxm = lin(g, im, j, k), lym = lin(g, i, jm, k), lzm = lin(g, i, j, km);
         pex[t] = 0.5f * (ex[t] + ex[lxm]);

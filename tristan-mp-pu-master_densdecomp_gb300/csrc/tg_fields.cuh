@@ -66,27 +66,28 @@ inline void ghost_plan(const Geom &g, GhostKind kind, GhostAxis ax[3], long long
 __device__ __forceinline__ void ghost_one(const Geom &g, float *a, float *b, float *c, const GhostAxis &ax,
                                           const GhostAxis &ay, const GhostAxis &az, long long nX, long long nY,
                                           long long t) {
+    // 32-bit index arithmetic: the ghost shell holds fewer than 2^31 cells
     int i, j, k;
     if (t < nX) {  // x-target layers, every j, k
-        long long r = t;
-        i = ax.target((int)(r % ax.nt));
+        int r = (int)t;
+        i = ax.target(r % ax.nt);
         r /= ax.nt;
-        j = (int)(r % g.my) + 1;
-        k = (int)(r / g.my) + 1;
+        j = r % g.my + 1;
+        k = r / g.my + 1;
     } else if (t < nX + nY) {  // x non-target, y-target, every k
-        long long r = t - nX;
+        int r = (int)(t - nX);
         const int nnx = g.mx - ax.nt;
-        i = ax.nontarget((int)(r % nnx));
+        i = ax.nontarget(r % nnx);
         r /= nnx;
-        j = ay.target((int)(r % ay.nt));
-        k = (int)(r / ay.nt) + 1;
+        j = ay.target(r % ay.nt);
+        k = r / ay.nt + 1;
     } else {  // x, y non-target, z-target
-        long long r = t - nX - nY;
+        int r = (int)(t - nX - nY);
         const int nnx = g.mx - ax.nt, nny = g.my - ay.nt;
-        i = ax.nontarget((int)(r % nnx));
+        i = ax.nontarget(r % nnx);
         r /= nnx;
-        j = ay.nontarget((int)(r % nny));
-        k = az.target((int)(r / nny));
+        j = ay.nontarget(r % nny);
+        k = az.target(r / nny);
     }
     const long long dst = lin(g, i, j, k);
     const long long src = lin(g, ax.image(i), ay.image(j), az.image(k));
@@ -128,10 +129,12 @@ template <int DIM>
 __device__ __forceinline__ void advance_b_one(const Geom &g, const Box &bx_, float cst, const float *__restrict__ ex,
                                               const float *__restrict__ ey, const float *__restrict__ ez, float *bx,
                                               float *by, float *bz, long long t) {
-    const int i = (int)(t % bx_.ni) + bx_.i1;
-    const long long r = t / bx_.ni;
-    const int j = (int)(r % bx_.nj) + bx_.j1;
-    const int k = (int)(r / bx_.nj) + bx_.k1;
+    // 32-bit index arithmetic: a box holds fewer than 2^31 cells
+    const int ti = (int)t;
+    const int i = ti % bx_.ni + bx_.i1;
+    const int r = ti / bx_.ni;
+    const int j = r % bx_.nj + bx_.j1;
+    const int k = r / bx_.nj + bx_.k1;
     const long long l = lin(g, i, j, k);
     const long long lx = l + 1, ly = l + g.sy;
     if (DIM == 3) {
@@ -150,10 +153,11 @@ template <int DIM>
 __device__ __forceinline__ void advance_e_one(const Geom &g, const Box &b_, float cst, float *ex, float *ey, float *ez,
                                               const float *__restrict__ bx, const float *__restrict__ by,
                                               const float *__restrict__ bz, long long t) {
-    const int i = (int)(t % b_.ni) + b_.i1;
-    const long long r = t / b_.ni;
-    const int j = (int)(r % b_.nj) + b_.j1;
-    const int k = (int)(r / b_.nj) + b_.k1;
+    const int ti = (int)t;
+    const int i = ti % b_.ni + b_.i1;
+    const int r = ti / b_.ni;
+    const int j = r % b_.nj + b_.j1;
+    const int k = r / b_.nj + b_.k1;
     const long long l = lin(g, i, j, k);
     const long long lx = l - 1, ly = l - g.sy;
     if (DIM == 3) {
@@ -180,10 +184,10 @@ __device__ __forceinline__ void fold_one(const Geom &g, int axis, int m, int ng,
     const int nb1 = ng / 2 + 1;
     const int n1 = axis == 0 ? g.my : g.mx;  // first face extent
     const int n2 = axis == 2 ? g.my : g.mz;  // second face extent
-    const long long face = (long long)n1 * n2;
-    const int layer = (int)(t / face) + (slab == 1 ? nb1 : 0);
-    const long long f = t % face;
-    const int p = (int)(f % n1) + 1, q = (int)(f / n1) + 1;
+    const int face = n1 * n2, ti = (int)t;
+    const int layer = ti / face + (slab == 1 ? nb1 : 0);
+    const int f = ti % face;
+    const int p = f % n1 + 1, q = f / n1 + 1;
     (void)n2;
     int tgt, src;
     if (layer < nb1) {
@@ -268,10 +272,11 @@ __device__ __forceinline__ void filter_one(const Geom &g, const float *__restric
     const int ilo = g.ng / 2 + 1, ihi = g.mx - (g.ng / 2 + 1);
     const int jlo = g.ng / 2 + 1, jhi = g.my - (g.ng / 2 + 1);
     const int klo = DIM == 3 ? g.ngz / 2 + 1 : 1, khi = DIM == 3 ? g.mz - (g.ngz / 2 + 1) : 1;
-    const int i = (int)(t % g.mx) + 1;
-    const long long r = t / g.mx;
-    const int j = (int)(r % g.my) + 1;
-    const int k = (int)(r / g.my) + 1;
+    const int ti = (int)t;
+    const int i = ti % g.mx + 1;
+    const int r = ti / g.mx;
+    const int j = r % g.my + 1;
+    const int k = r / g.my + 1;
     const bool in_ik = i >= ilo && i <= ihi && k >= klo && k <= khi;
     const bool in_xy = in_ik && j >= jlo && j <= jhi;
     const bool in_z = in_ik && j >= jlo && j <= jhi + 2;

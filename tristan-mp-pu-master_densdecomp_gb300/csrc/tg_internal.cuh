@@ -29,7 +29,7 @@ namespace tg {
 #define TG_NEGSIXTH (-0x1.555556p-3f)
 
 // device status bits
-enum : int32_t { ST_BOUNDS = 1, ST_NAN = 2, ST_OVERFLOW = 4, ST_WINDOW = 8 };
+enum : int32_t { ST_BOUNDS = 1, ST_NAN = 2, ST_OVERFLOW = 4, ST_WINDOW = 8, ST_CHARGE_GRID = 16 };
 
 // ---------------------------------------------------------------------------
 // Geometry of one domain (derived once at tg_init)
@@ -456,7 +456,7 @@ struct DiagLaunch {
     float mass[2];
     const float *f[6];
     unsigned long long *rhofx;  // periodic interior, fixed point
-    double *rho[2];             // periodic interior, FP64 ping-pong
+    double *rho[2];             // periodic interior ping-pong (holds the int64 charge grid)
     double *acc;                // 16 accumulators
     double *hist;               // history ring [hist_cap][16]
     int hist_cap;
