@@ -40,6 +40,10 @@ namespace tg {
 
 #define TG_ENS_CHUNK 4096   // cells per CTA of a batched field kernel
 #define TG_ENS_DIAG_CAP 8   // diagnostics records kept per box
+// resident CTAs per SM of the persistent tile kernels (as the 2D tile kernel)
+#ifndef TG_ENS_MINB
+#define TG_ENS_MINB TG_TILES_MINB_2D
+#endif
 
 // per-box constants of the batched field kernels
 struct EnsBox {
@@ -134,7 +138,7 @@ __global__ void __launch_bounds__(256) k_ens_fixed_to_float(const EnsBox *__rest
 // order's work queue; a CTA keeps the arguments of its current box in
 // shared memory. The three orders run as concurrent branches of the lap.
 template <int ORDER, bool FIXED>
-__global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
+__global__ void __launch_bounds__(256, TG_ENS_MINB)
     k_ens_tiles(const TileArgs *__restrict__ boxes, const int2 *__restrict__ work, int nwork, int *queue) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(16) TileArgs sa;
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
 #define TG_ENS_CONST_BOXES 72
 __constant__ TileArgs c_ens_targs[TG_ENS_CONST_BOXES];
 template <int ORDER, bool FIXED>
-__global__ void __launch_bounds__(256, TG_TILES_MINB_2D)
+__global__ void __launch_bounds__(256, TG_ENS_MINB)
     k_ens_tiles_c(const int2 *__restrict__ work, int nwork, int *queue) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;

@@ -173,6 +173,11 @@ struct WindowSink {
     __device__ __forceinline__ int index(int i, int j, int k) const {
         return (i - wx0) + wx * ((j - wy0) + wy * (k - wz0));
     }
+    // add v at window index widx: the caller has shown that the cell lies
+    // in the window and that |v| * scale < 2^30
+    __device__ __forceinline__ void add_win(int comp, int widx, float v) {
+        fx_add_shared(lo, hi, comp * wcells + widx, to_fixed32(v * scale));
+    }
     // add v at window index widx when in (the cell is in the window),
     // otherwise at cell (i, j, k) of the global arrays
     __device__ __forceinline__ void add_at(int comp, int widx, bool in, int i, int j, int k, float v) {
@@ -263,6 +268,130 @@ __device__ __forceinline__ bool wall_reflect(Sink &sink, float c, float gammawal
 // arithmetic, including the carries that are not reset between rows (x)
 // and planes (y) (Q4). Cells are visited in the reference's order.
 // ---------------------------------------------------------------------------
+// slack on the displacement bound of the lean deposit (covers the FP32
+// residue of the carries, < 1e-5 of |q|) and the limit of one exact window
+// update in fixed-point units
+#define TG_LEAN_SLACK 0x1p-10f
+#define TG_LEAN_LIMIT 1073741824.0f
+
+// One contribution of the Esirkepov loops. LEAN: every cell of the stencil
+// lies in the tile window and no contribution reaches 2^30 units, so v goes
+// straight into the window; otherwise each cell is checked (add_at).
+template <bool LEAN, class Sink>
+__device__ __forceinline__ void dep_add(Sink &sink, int comp, int widx, bool in, int i, int j, int k, float v) {
+    if (LEAN)
+        sink.add_win(comp, widx, v);
+    else
+        sink.add_at(comp, widx, in, i, j, k, v);
+}
+
+// 2D loops of densdecomp_{1,2,3}ord: rows rolled (code size), the row's
+// cells unrolled (carries in registers)
+template <int U, bool LEAN, class Sink>
+__device__ __forceinline__ void esirkepov2_loops(Sink &sink, const float *S1x, const float *S2x, const float *S1y,
+                                                 const float *S2y, int nx, int ny, int ibase, int jbase, float q,
+                                                 float deltaz, bool in) {
+    float cxp = 0.0f;
+    float cyp[U];
+#pragma unroll
+    for (int r = 0; r < U; r++) cyp[r] = 0.0f;
+#pragma unroll 1
+    for (int ry = 0; ry < ny; ry++) {
+        const float s1y = sel<U>(S1y, ry), dSy = sel<U>(S2y, ry) - s1y;
+        const float wy = s1y + TG_HALF * dSy;
+        const int row = sink.index(ibase, jbase + ry, 1);
+#pragma unroll
+        for (int rx = 0; rx < U; rx++) {
+            if (rx < nx) {
+                const float s1x = S1x[rx], dSx = S2x[rx] - S1x[rx];
+                const float cx = q * (dSx * wy) + cxp;
+                const float cy = q * (dSy * (s1x + TG_HALF * dSx)) + cyp[rx];
+                const float cz = -(q * deltaz *
+                                   (s1x * s1y + TG_HALF * dSx * s1y + TG_HALF * s1x * dSy + TG_THIRD * dSx * dSy));
+                dep_add<LEAN>(sink, 0, row + rx, in, ibase + rx, jbase + ry, 1, cx);
+                dep_add<LEAN>(sink, 1, row + rx, in, ibase + rx, jbase + ry, 1, cy);
+                dep_add<LEAN>(sink, 2, row + rx, in, ibase + rx, jbase + ry, 1, cz);
+                cxp = cx;
+                cyp[rx] = cy;
+            }
+        }
+    }
+}
+
+// 3D loops. The three components' carries form independent chains: cx one
+// chain over all cells in the reference's (z, y, x) order, cy one chain per
+// x slot over (z, y), cz one chain per (x, y) slot over z. Each chain is
+// walked in its own order below, so every cell gets exactly the reference's
+// value while only one row of carries is live at a time (the window sums
+// are order independent).
+template <int U, bool LEAN, class Sink>
+__device__ __forceinline__ void esirkepov3_loops(Sink &sink, const float *S1x, const float *S2x, const float *S1y,
+                                                 const float *S2y, const float *S1z, const float *S2z, int nx,
+                                                 int ny, int nz, int ibase, int jbase, int kbase, float q, bool in) {
+    float cxp = 0.0f;
+    float cyp[U];
+#pragma unroll
+    for (int r = 0; r < U; r++) cyp[r] = 0.0f;
+    // cx and cy: planes and rows rolled, the row's cells unrolled
+#pragma unroll 1
+    for (int rz = 0; rz < nz; rz++) {
+        const float s1z = sel<U>(S1z, rz);
+        const float dSz = sel<U>(S2z, rz) - s1z;
+        float wxz[U];
+#pragma unroll
+        for (int rx = 0; rx < U; rx++) {
+            const float dSx = S2x[rx] - S1x[rx];
+            wxz[rx] = S1x[rx] * s1z + TG_HALF * dSx * s1z + TG_HALF * S1x[rx] * dSz + TG_THIRD * dSx * dSz;
+        }
+#pragma unroll 1
+        for (int ry = 0; ry < ny; ry++) {
+            const float s1y = sel<U>(S1y, ry);
+            const float dSy = sel<U>(S2y, ry) - s1y;
+            const float wyz = s1y * s1z + TG_HALF * dSy * s1z + TG_HALF * s1y * dSz + TG_THIRD * dSy * dSz;
+            const int row = sink.index(ibase, jbase + ry, kbase + rz);
+#pragma unroll
+            for (int rx = 0; rx < U; rx++) {
+                if (rx < nx) {
+                    const float dSx = S2x[rx] - S1x[rx];
+                    const float cx = q * (dSx * wyz) + cxp;
+                    const float cy = q * (dSy * wxz[rx]) + cyp[rx];
+                    dep_add<LEAN>(sink, 0, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cx);
+                    dep_add<LEAN>(sink, 1, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cy);
+                    cxp = cx;
+                    cyp[rx] = cy;
+                }
+            }
+        }
+    }
+    // cz: rows rolled, planes rolled inside, the row's cells unrolled
+#pragma unroll 1
+    for (int ry = 0; ry < ny; ry++) {
+        const float s1y = sel<U>(S1y, ry);
+        const float dSy = sel<U>(S2y, ry) - s1y;
+        float wxy[U], czp[U];
+#pragma unroll
+        for (int rx = 0; rx < U; rx++) {
+            const float dSx = S2x[rx] - S1x[rx];
+            wxy[rx] = S1x[rx] * s1y + TG_HALF * dSx * s1y + TG_HALF * S1x[rx] * dSy + TG_THIRD * dSx * dSy;
+            czp[rx] = 0.0f;
+        }
+#pragma unroll 1
+        for (int rz = 0; rz < nz; rz++) {
+            const float s1z = sel<U>(S1z, rz);
+            const float dSz = sel<U>(S2z, rz) - s1z;
+            const int row = sink.index(ibase, jbase + ry, kbase + rz);
+#pragma unroll
+            for (int rx = 0; rx < U; rx++) {
+                if (rx < nx) {
+                    const float cz = q * (dSz * wxy[rx]) + czp[rx];
+                    dep_add<LEAN>(sink, 2, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cz);
+                    czp[rx] = cz;
+                }
+            }
+        }
+    }
+}
+
 template <int DIM, int ORDER, class Sink>
 __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, float z2, float x1, float y1,
                                           float z1, float q, Sink &sink, int *status) {
@@ -298,41 +427,21 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
         S2y[r] = pick<NS>(w2y, r, b2y - loy);
     }
     const int ibase = i1 - 3 + lox, jbase = j1 - 3 + loy;
-    float cxp = 0.0f;
-    float cyp[U];
-#pragma unroll
-    for (int r = 0; r < U; r++) cyp[r] = 0.0f;
-
+    // The partial sums of S2 - S1 along an axis are bounded by the
+    // displacement d on that axis and the weights of the other axes by 1, so
+    // every contribution (carries included) is below |q| (d + FP32 residue);
+    // with that under 2^30 units and the whole stencil in the tile window
+    // (almost every particle: the window covers the drift since the last
+    // sort) the loops add into the window without per-cell checks.
+    const float bound = fabsf(q) * sink.scale;
     if (DIM == 2) {
         const float deltaz = z2 - z1;
-        // the whole stencil in the tile window (almost always): cells are
-        // addressed from the row's window index, without per-cell checks
         const bool in = sink.fits(ibase, jbase, 1, nx, ny, 1);
-        // rows rolled (code size), the row's cells unrolled (carries in registers)
-#pragma unroll 1
-        for (int ry = 0; ry < ny; ry++) {
-            {
-                const float s1y = sel<U>(S1y, ry), dSy = sel<U>(S2y, ry) - s1y;
-                const float wy = s1y + TG_HALF * dSy;
-                const int row = sink.index(ibase, jbase + ry, 1);
-#pragma unroll
-                for (int rx = 0; rx < U; rx++) {
-                    if (rx < nx) {
-                        const float s1x = S1x[rx], dSx = S2x[rx] - S1x[rx];
-                        const float cx = q * (dSx * wy) + cxp;
-                        const float cy = q * (dSy * (s1x + TG_HALF * dSx)) + cyp[rx];
-                        const float cz = -(q * deltaz *
-                                           (s1x * s1y + TG_HALF * dSx * s1y + TG_HALF * s1x * dSy +
-                                            TG_THIRD * dSx * dSy));
-                        sink.add_at(0, row + rx, in, ibase + rx, jbase + ry, 1, cx);
-                        sink.add_at(1, row + rx, in, ibase + rx, jbase + ry, 1, cy);
-                        sink.add_at(2, row + rx, in, ibase + rx, jbase + ry, 1, cz);
-                        cxp = cx;
-                        cyp[rx] = cy;
-                    }
-                }
-            }
-        }
+        const float d = fmaxf(fmaxf(fabsf(x2 - x1), fabsf(y2 - y1)), fabsf(deltaz));
+        if (in && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
+            esirkepov2_loops<U, true>(sink, S1x, S2x, S1y, S2y, nx, ny, ibase, jbase, q, deltaz, true);
+        else
+            esirkepov2_loops<U, false>(sink, S1x, S2x, S1y, S2y, nx, ny, ibase, jbase, q, deltaz, in);
     } else {
         const float dz1 = z1 - truncf(z1), dz2 = z2 - truncf(z2);
         float w1z[NS], w2z[NS];
@@ -350,70 +459,11 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
             S1z[r] = pick<NS>(w1z, r, b1z - loz);
             S2z[r] = pick<NS>(w2z, r, b2z - loz);
         }
-        // The three components' carries form independent chains: cx one
-        // chain over all cells in the reference's (z, y, x) order, cy one
-        // chain per x slot over (z, y), cz one chain per (x, y) slot over z.
-        // Each chain is walked in its own order below, so every cell gets
-        // exactly the reference's value while only one row of carries is
-        // live at a time (the window sums are order independent).
-        // cx and cy: planes and rows rolled, the row's cells unrolled
-#pragma unroll 1
-        for (int rz = 0; rz < nz; rz++) {
-            const float s1z = sel<U>(S1z, rz);
-            const float dSz = sel<U>(S2z, rz) - s1z;
-            float wxz[U];
-#pragma unroll
-            for (int rx = 0; rx < U; rx++) {
-                const float dSx = S2x[rx] - S1x[rx];
-                wxz[rx] = S1x[rx] * s1z + TG_HALF * dSx * s1z + TG_HALF * S1x[rx] * dSz + TG_THIRD * dSx * dSz;
-            }
-#pragma unroll 1
-            for (int ry = 0; ry < ny; ry++) {
-                const float s1y = sel<U>(S1y, ry);
-                const float dSy = sel<U>(S2y, ry) - s1y;
-                const float wyz = s1y * s1z + TG_HALF * dSy * s1z + TG_HALF * s1y * dSz + TG_THIRD * dSy * dSz;
-                const int row = sink.index(ibase, jbase + ry, kbase + rz);
-#pragma unroll
-                for (int rx = 0; rx < U; rx++) {
-                    if (rx < nx) {
-                        const float dSx = S2x[rx] - S1x[rx];
-                        const float cx = q * (dSx * wyz) + cxp;
-                        const float cy = q * (dSy * wxz[rx]) + cyp[rx];
-                        sink.add_at(0, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cx);
-                        sink.add_at(1, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cy);
-                        cxp = cx;
-                        cyp[rx] = cy;
-                    }
-                }
-            }
-        }
-        // cz: rows rolled, planes rolled inside, the row's cells unrolled
-#pragma unroll 1
-        for (int ry = 0; ry < ny; ry++) {
-            const float s1y = sel<U>(S1y, ry);
-            const float dSy = sel<U>(S2y, ry) - s1y;
-            float wxy[U], czp[U];
-#pragma unroll
-            for (int rx = 0; rx < U; rx++) {
-                const float dSx = S2x[rx] - S1x[rx];
-                wxy[rx] = S1x[rx] * s1y + TG_HALF * dSx * s1y + TG_HALF * S1x[rx] * dSy + TG_THIRD * dSx * dSy;
-                czp[rx] = 0.0f;
-            }
-#pragma unroll 1
-            for (int rz = 0; rz < nz; rz++) {
-                const float s1z = sel<U>(S1z, rz);
-                const float dSz = sel<U>(S2z, rz) - s1z;
-                const int row = sink.index(ibase, jbase + ry, kbase + rz);
-#pragma unroll
-                for (int rx = 0; rx < U; rx++) {
-                    if (rx < nx) {
-                        const float cz = q * (dSz * wxy[rx]) + czp[rx];
-                        sink.add_at(2, row + rx, in, ibase + rx, jbase + ry, kbase + rz, cz);
-                        czp[rx] = cz;
-                    }
-                }
-            }
-        }
+        const float d = fmaxf(fmaxf(fabsf(x2 - x1), fabsf(y2 - y1)), fabsf(z2 - z1));
+        if (in && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
+            esirkepov3_loops<U, true>(sink, S1x, S2x, S1y, S2y, S1z, S2z, nx, ny, nz, ibase, jbase, kbase, q, true);
+        else
+            esirkepov3_loops<U, false>(sink, S1x, S2x, S1y, S2y, S1z, S2z, nx, ny, nz, ibase, jbase, kbase, q, in);
     }
 }
 
@@ -436,6 +486,34 @@ __device__ __forceinline__ long long interior_index(const Geom &g, int ii, int j
     return wrap_i(ii, lo, nx) + (long long)nx * (wrap_i(jj, lo, ny) + (long long)ny * (DIM == 3 ? wrap_i(kk, loz, nz) : 0));
 }
 
+// rows of rho_deposit: LEAN adds into the window without per-node checks
+template <int DIM, int NS, bool LEAN>
+__device__ __forceinline__ void rho_rows(const Geom &g, float fx_scale, int i, int j, int k, int bx, int by, int bz,
+                                         const float *wx, const float *wy, const float *wz, float q, unsigned *rlo,
+                                         int *rhi, int ra0, int rb0, int rc0, bool in,
+                                         unsigned long long *rhofx) {
+    constexpr int NZ = DIM == 3 ? NS : 1;
+#pragma unroll 1
+    for (int c = 0; c < NZ; c++) {
+        const float wzc = sel<NS>(wz, c);
+#pragma unroll
+        for (int b = 0; b < NS; b++) {
+            const float qyz = q * wy[b] * wzc;
+            const int row = ra0 + g.wx * (rb0 + b + g.wy * (rc0 + c));
+#pragma unroll
+            for (int aa = 0; aa < NS; aa++) {
+                const float xs = qyz * wx[aa] * fx_scale;
+                if (LEAN || (in && fabsf(xs) < TG_LEAN_LIMIT)) {
+                    fx_add_shared(rlo, rhi, row + aa, to_fixed32(xs));
+                } else {
+                    const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
+                    atomicAdd(rhofx + interior_index<DIM>(g, ii, jj, kk), (unsigned long long)to_fixed(xs));
+                }
+            }
+        }
+    }
+}
+
 // charge of one particle at node offsets (ox,oy,oz) of node (i,j,k), with
 // the deposit's B-spline: FP32 products, one rounding to fixed point, into
 // the shared window (wx0.. origin) or, outside it, the periodic interior
@@ -452,29 +530,16 @@ __device__ __forceinline__ void rho_deposit(const Geom &g, float fx_scale, int i
     else wz[0] = 1.0f;
     constexpr int NZ = DIM == 3 ? NS : 1;
     // the whole NS^dims box in the window (almost always): nodes are
-    // addressed from the row's window index without per-node checks
+    // addressed from the row's window index; the weights' products stay
+    // below 1 + 2^-20, so with |q| under 2^30 units (less the slack) no
+    // node needs a magnitude check either
     const int ra0 = i - 3 + bx - wx0, rb0 = j - 3 + by - wy0, rc0 = (DIM == 3 ? k - 3 + bz : 1) - wz0;
     const bool in = use_win && ra0 >= 0 && rb0 >= 0 && rc0 >= 0 && ra0 + NS <= g.wx && rb0 + NS <= g.wy &&
                     rc0 + NZ <= g.wz;
-#pragma unroll 1
-    for (int c = 0; c < NZ; c++) {
-        const float wzc = sel<NS>(wz, c);
-#pragma unroll
-        for (int b = 0; b < NS; b++) {
-            const float qyz = q * wy[b] * wzc;
-            const int row = ra0 + g.wx * (rb0 + b + g.wy * (rc0 + c));
-#pragma unroll
-            for (int aa = 0; aa < NS; aa++) {
-                const float xs = qyz * wx[aa] * fx_scale;
-                if (in && fabsf(xs) < 1073741824.0f) {
-                    fx_add_shared(rlo, rhi, row + aa, to_fixed32(xs));
-                } else {
-                    const int ii = i - 3 + bx + aa, jj = j - 3 + by + b, kk = DIM == 3 ? k - 3 + bz + c : 1;
-                    atomicAdd(rhofx + interior_index<DIM>(g, ii, jj, kk), (unsigned long long)to_fixed(xs));
-                }
-            }
-        }
-    }
+    if (in && fabsf(q) * fx_scale * (1.0f + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
+        rho_rows<DIM, NS, true>(g, fx_scale, i, j, k, bx, by, bz, wx, wy, wz, q, rlo, rhi, ra0, rb0, rc0, true, rhofx);
+    else
+        rho_rows<DIM, NS, false>(g, fx_scale, i, j, k, bx, by, bz, wx, wy, wz, q, rlo, rhi, ra0, rb0, rc0, in, rhofx);
 }
 
 template <int DIM>
@@ -514,16 +579,18 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
     }
 }
 
-// resident CTAs per SM the register budget is sized for: 2D kernels run
-// best at 4 (64 registers, small spills), 3D kernels carry more state
+// resident CTAs per SM the register budget is sized for (measured): 2D
+// kernels at 3 (80 registers; 4 CTAs at 64 registers spill the lean and the
+// checked deposit loops), 3D kernels at 2 (126 registers; 3 CTAs at 80
+// spill)
 #ifndef TG_TILES_MINB_2D
-#define TG_TILES_MINB_2D 4
+#define TG_TILES_MINB_2D 3
 #endif
 #ifndef TG_TILES_MINB_3D
 #define TG_TILES_MINB_3D 2
 #endif
-// threads per tile CTA: 3D tiles hold more particles and a larger window,
-// so two CTAs of 512 threads share an SM's shared memory
+// threads per tile CTA in 3D (the window of a 16 x 8 x 4 order-2 tile is
+// 59 KB, so three CTAs fit in an SM's shared memory)
 #ifndef TG_TILE_THREADS_3D
 #define TG_TILE_THREADS_3D 256
 #endif
