@@ -252,6 +252,7 @@ def run_e2e(cfg, ions, lecs, e2e_steps, host_parts, device):
     sim.sync_from_host(SYNC_ALL)
     sim.step_host(1)
     h2d, d2h = sim.host_bytes(up), sim.host_bytes(SYNC_ALL)
+    huge = sim.host_huge_fraction()
     # one tg_step_host call per lap: E, B and the records up, the lap,
     # everything back, as the reference's main loop would drive it
     t0 = time.perf_counter()
@@ -259,32 +260,52 @@ def run_e2e(cfg, ions, lecs, e2e_steps, host_parts, device):
         sim.step_host(1)
     dt = time.perf_counter() - t0
     sim.close()
-    return dt, h2d, d2h
+    return dt, h2d, d2h, huge
 
 
 def copy_only_ms(h2d, d2h, device, reps=3):
     """the same bytes moved between page-locked host memory and the device
     with nothing else running, both directions at once (one stream each):
-    the link's bound for one end-to-end step"""
+    the link's bound for one end-to-end step. The host buffers come from the
+    same allocator as GpuSim's pinned host arrays (anonymous memory advised
+    for huge pages, then cudaHostRegister), so both see the same kind of
+    pages. Returns (ms, share of the buffers on huge pages)."""
+    import ctypes
     import torch
+    from tristan_gb300 import gpu
     dev = torch.device("cuda", device)
-    hu = torch.empty(h2d, dtype=torch.uint8, pin_memory=True)
-    hd = torch.empty(d2h, dtype=torch.uint8, pin_memory=True)
+    rt = gpu._cudart_lib()
+    rt.cudaMemcpyAsync.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                   ctypes.c_void_p]
+    rt.cudaMemcpyAsync.restype = ctypes.c_int
+    hu = gpu._host_array(h2d, np.uint8, True)
+    hd = gpu._host_array(d2h, np.uint8, True)
+    hu[:] = 1
+    hd[:] = 1
+    huge = gpu.huge_page_fraction([hu, hd])
+    for a in (hu, hd):
+        if rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0) != 0:
+            raise RuntimeError("cudaHostRegister failed")
     du = torch.empty(h2d, dtype=torch.uint8, device=dev)
     dd = torch.empty(d2h, dtype=torch.uint8, device=dev)
     s_up, s_down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    for r in range(reps + 1):
-        if r == 1:
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-        with torch.cuda.stream(s_up):
-            du.copy_(hu, non_blocking=True)
-        with torch.cuda.stream(s_down):
-            hd.copy_(dd, non_blocking=True)
-    torch.cuda.synchronize(dev)
-    ms = (time.perf_counter() - t0) / reps * 1e3
-    del hu, hd, du, dd
-    return ms
+    try:
+        for r in range(reps + 1):
+            if r == 1:
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+            if rt.cudaMemcpyAsync(du.data_ptr(), hu.ctypes.data, h2d, 1, s_up.cuda_stream) != 0:
+                raise RuntimeError("cudaMemcpyAsync failed")
+            if rt.cudaMemcpyAsync(hd.ctypes.data, dd.data_ptr(), d2h, 2, s_down.cuda_stream) != 0:
+                raise RuntimeError("cudaMemcpyAsync failed")
+        torch.cuda.synchronize(dev)
+        ms = (time.perf_counter() - t0) / reps * 1e3
+    finally:
+        torch.cuda.synchronize(dev)
+        for a in (hu, hd):
+            rt.cudaHostUnregister(a.ctypes.data)
+    del du, dd
+    return ms, huge
 
 
 def cpu_baseline(cfg, ions, lecs, steps):
@@ -358,14 +379,18 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
         ms_f = allreduce_max(ms_f, ws, args.impl)
         fixed = {"value": ws * n_p * steps / (ms_f / 1e3), "ms_per_step": ms_f / steps,
                  "particle_kernel_ms": ph_f["particles"], "deposit": DEPOSIT_FIXED}
-    dt_e2e, h2d, d2h = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
+    dt_e2e, h2d, d2h, huge_lap = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
     ms_e2e = dt_e2e / e2e_steps * 1e3
-    ms_link = copy_only_ms(h2d, d2h, device)
+    ms_link, huge_link = copy_only_ms(h2d, d2h, device)
     e2e = {"value": ws * n_p * e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e,
            "link": {"bound": "host link (NVLink-C2C), both directions at once",
                     "copy_only_ms": ms_link, "achieved_gbs": (h2d + d2h) / ms_e2e / 1e6,
-                    "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e},
+                    "peak_gbs": (h2d + d2h) / ms_link / 1e6, "frac": ms_link / ms_e2e,
+                    # the host link moves fewer bytes per second from base
+                    # pages when both directions run; the kernel grants
+                    # huge pages as free memory allows
+                    "host_huge_page_share": {"lap_arrays": huge_lap, "copy_buffers": huge_link}},
            # the lap cannot take less than the longer of its copies and its
            # device-resident lap (the two overlap part by part)
            "lap_bound_ms": max(ms_link, ms / steps), "frac_of_lap_bound": max(ms_link, ms / steps) / ms_e2e,

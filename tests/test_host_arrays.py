@@ -24,3 +24,12 @@ def test_unpinned_host_arrays_are_plain():
     a = gpu._host_array(10, np.float32, False)
     assert isinstance(a, np.ndarray) and a.shape == (10,) and not a.any()
     assert gpu._host_array(0, np.float32, True).shape == (0,)
+
+
+def test_huge_page_fraction_reads_the_arrays_mappings():
+    a = gpu._host_array(3 * gpu._huge_page_bytes() // 4, np.float32, True)
+    a[:] = 1.0  # touch every page
+    f = gpu.huge_page_fraction([a])
+    assert f is None or 0.0 <= f <= 1.0
+    assert gpu.huge_page_fraction([]) is None
+    assert gpu.huge_page_fraction([np.zeros(0, np.float32)]) is None

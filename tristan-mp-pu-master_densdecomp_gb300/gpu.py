@@ -353,6 +353,36 @@ def _host_array(n: int, dtype, pinned: bool) -> np.ndarray:
     return raw[off: off + nbytes].view(dtype)
 
 
+def huge_page_fraction(arrays) -> float | None:
+    """share of the memory mappings holding `arrays` that the kernel backs
+    with transparent huge pages (AnonHugePages / Size in /proc/self/smaps);
+    None where smaps cannot be read"""
+    spans = [(a.ctypes.data, a.ctypes.data + a.nbytes) for a in arrays if a.nbytes]
+    if not spans:
+        return None
+    try:
+        with open("/proc/self/smaps") as f:
+            lines = f.read().splitlines()
+    except OSError:
+        return None
+    size = huge = 0
+    hit = False
+    for line in lines:
+        head = line.split(None, 1)[0] if line else ""
+        if "-" in head and ":" not in head:
+            try:
+                lo, hi = (int(v, 16) for v in head.split("-"))
+            except ValueError:
+                hit = False
+                continue
+            hit = any(lo < e and s < hi for s, e in spans)
+        elif hit and head == "Size:":
+            size += int(line.split()[1])
+        elif hit and head == "AnonHugePages:":
+            huge += int(line.split()[1])
+    return huge / size if size else None
+
+
 class GpuSim:
     """One device domain plus the host arrays it syncs with. ``pinned``
     puts the host arrays on huge pages and page-locks them
@@ -392,6 +422,10 @@ class GpuSim:
             for arr in getattr(self, "_pinned", []):
                 _cudart_lib().cudaHostUnregister(arr.ctypes.data)
             self._pinned = []
+
+    def host_huge_fraction(self) -> float | None:
+        """share of the host arrays' mappings on transparent huge pages"""
+        return huge_page_fraction([self.p] + [self.fields[k] for k in FIELD_NAMES])
 
     def host_bytes(self, mask: int) -> int:
         """bytes one sync of `mask` moves (particles at the current counts)"""
