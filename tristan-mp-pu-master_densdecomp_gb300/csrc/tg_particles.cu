@@ -82,21 +82,26 @@ __global__ void k_tile_scatter(Geom g, Species src, Species dst, const long long
          n += (long long)gridDim.x * blockDim.x) {
         const int cell = src.cell[n];
         if (cell < 0) continue;
+        // the record is read before its slot is claimed, so the loads'
+        // latency overlaps the atomic's round trip
+        const float ox = src.ox[n], oy = src.oy[n], oz = src.oz[n];
+        const float u = src.u[n], v = src.v[n], w = src.w[n], ch = src.ch[n];
+        const int32_t ind = src.ind[n], proc = src.proc[n], spl = src.splitlev[n];
         int i, j, k;
         cell_ijk(g, cell, i, j, k);
         const int t = tile_of(g, i, j, k);
         const long long d = (long long)start[t] + agg_inc(cursor, t);
         dst.cell[d] = cell;
-        dst.ox[d] = src.ox[n];
-        dst.oy[d] = src.oy[n];
-        dst.oz[d] = src.oz[n];
-        dst.u[d] = src.u[n];
-        dst.v[d] = src.v[n];
-        dst.w[d] = src.w[n];
-        dst.ch[d] = src.ch[n];
-        dst.ind[d] = src.ind[n];
-        dst.proc[d] = src.proc[n];
-        dst.splitlev[d] = src.splitlev[n];
+        dst.ox[d] = ox;
+        dst.oy[d] = oy;
+        dst.oz[d] = oz;
+        dst.u[d] = u;
+        dst.v[d] = v;
+        dst.w[d] = w;
+        dst.ch[d] = ch;
+        dst.ind[d] = ind;
+        dst.proc[d] = proc;
+        dst.splitlev[d] = spl;
     }
 }
 

@@ -433,13 +433,17 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
     // with that under 2^30 units and the whole stencil in the tile window
     // (almost every particle: the window covers the drift since the last
     // sort) the loops add into the window without per-cell checks.
+    // The lean loops walk at most NS + 1 cells per axis (a move of under
+    // one cell shifts the shape's first node by one at most), so for order
+    // 2 they unroll four x cells instead of the five of the general loops.
+    constexpr int UL = ShapeN<ORDER>::NS + 1;
     const float bound = fabsf(q) * sink.scale;
     if (DIM == 2) {
         const float deltaz = z2 - z1;
         const bool in = sink.fits(ibase, jbase, 1, nx, ny, 1);
         const float d = fmaxf(fmaxf(fabsf(x2 - x1), fabsf(y2 - y1)), fabsf(deltaz));
-        if (in && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
-            esirkepov2_loops<U, true>(sink, S1x, S2x, S1y, S2y, nx, ny, ibase, jbase, q, deltaz, true);
+        if (in && nx <= UL && ny <= UL && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
+            esirkepov2_loops<UL, true>(sink, S1x, S2x, S1y, S2y, nx, ny, ibase, jbase, q, deltaz, true);
         else
             esirkepov2_loops<U, false>(sink, S1x, S2x, S1y, S2y, nx, ny, ibase, jbase, q, deltaz, in);
     } else {
@@ -460,8 +464,8 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
             S2z[r] = pick<NS>(w2z, r, b2z - loz);
         }
         const float d = fmaxf(fmaxf(fabsf(x2 - x1), fabsf(y2 - y1)), fabsf(z2 - z1));
-        if (in && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
-            esirkepov3_loops<U, true>(sink, S1x, S2x, S1y, S2y, S1z, S2z, nx, ny, nz, ibase, jbase, kbase, q, true);
+        if (in && nx <= UL && ny <= UL && nz <= UL && bound * (d + TG_LEAN_SLACK) < TG_LEAN_LIMIT)
+            esirkepov3_loops<UL, true>(sink, S1x, S2x, S1y, S2y, S1z, S2z, nx, ny, nz, ibase, jbase, kbase, q, true);
         else
             esirkepov3_loops<U, false>(sink, S1x, S2x, S1y, S2y, S1z, S2z, nx, ny, nz, ibase, jbase, kbase, q, in);
     }
