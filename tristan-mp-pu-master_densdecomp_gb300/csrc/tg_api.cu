@@ -48,7 +48,7 @@ struct tg_ctx {
     // device fields: ex ey ez bx by bz curx cury curz
     float *f[9] = {};
     float *ftmp[3] = {};   // filter ping-pong
-    float *prim[6] = {};   // 3D primal copies
+    float4 *prim = nullptr;  // 3D primal copies, two float4 per cell (interleaved)
     unsigned long long *fix[3] = {};
     // particles: [parity][species]
     Species sp[2][2];
@@ -316,7 +316,7 @@ extern "C" int tg_init(const tg_config *cfg, tg_ctx **out) {
     for (int a = 0; a < 9 && !r; a++) r = dalloc(ctx, &ctx->f[a], lot);
     for (int a = 0; a < 3 && !r; a++) r = dalloc(ctx, &ctx->ftmp[a], lot);
     if (g.dims == 3)
-        for (int a = 0; a < 6 && !r; a++) r = dalloc(ctx, &ctx->prim[a], lot);
+        r = dalloc(ctx, &ctx->prim, 2 * lot);
     if (ctx->P.fixed)
         for (int a = 0; a < 3 && !r; a++) r = dalloc(ctx, &ctx->fix[a], lot);
     for (int p = 0; p < 2 && !r; p++)
@@ -495,8 +495,7 @@ static TileArgs tile_args(tg_ctx *ctx, bool count_tiles) {
     a.P = ctx->P;
     a.f.ex = ctx->f[0]; a.f.ey = ctx->f[1]; a.f.ez = ctx->f[2];
     a.f.bx = ctx->f[3]; a.f.by = ctx->f[4]; a.f.bz = ctx->f[5];
-    a.f.pex = ctx->prim[0]; a.f.pey = ctx->prim[1]; a.f.pez = ctx->prim[2];
-    a.f.pbx = ctx->prim[3]; a.f.pby = ctx->prim[4]; a.f.pbz = ctx->prim[5];
+    a.f.prim = ctx->prim;
     for (int s = 0; s < 2; s++) {
         a.sp[s] = ctx->sp[ctx->par][s];
         a.tstart[s] = ctx->tstart[s];
@@ -706,8 +705,7 @@ extern "C" int tg_move(tg_ctx *ctx) {
     FieldPtrs fp;
     fp.ex = ctx->f[0]; fp.ey = ctx->f[1]; fp.ez = ctx->f[2];
     fp.bx = ctx->f[3]; fp.by = ctx->f[4]; fp.bz = ctx->f[5];
-    fp.pex = ctx->prim[0]; fp.pey = ctx->prim[1]; fp.pez = ctx->prim[2];
-    fp.pbx = ctx->prim[3]; fp.pby = ctx->prim[4]; fp.pbz = ctx->prim[5];
+    fp.prim = ctx->prim;
     if (ctx->g.dims == 3) CK(launch_primal(ctx->g, ctx->f, ctx->prim, ctx->st));
     for (int s = 0; s < 2; s++)
         CK(launch_push_flat(ctx->g, ctx->P, fp, ctx->sp[ctx->par][s], ctx->d_cnt + 2 * ctx->par + s,

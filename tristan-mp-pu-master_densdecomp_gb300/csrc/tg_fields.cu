@@ -291,8 +291,7 @@ cudaError_t launch_filter_pass(const Geom &g, float *const *in, float *const *ou
 // ---------------------------------------------------------------------------
 __global__ void k_primal(Geom g, const float *__restrict__ ex, const float *__restrict__ ey,
                          const float *__restrict__ ez, const float *__restrict__ bx, const float *__restrict__ by,
-                         const float *__restrict__ bz, float *pex, float *pey, float *pez, float *pbx, float *pby,
-                         float *pbz) {
+                         const float *__restrict__ bz, float4 *prim) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.lot;
          t += (long long)gridDim.x * blockDim.x) {
         const int ti = (int)t;  // fewer than 2^31 cells
@@ -302,18 +301,16 @@ __global__ void k_primal(Geom g, const float *__restrict__ ex, const float *__re
         const int k = r / g.my + 1;
         const int im = i == 1 ? g.mx : i - 1, jm = j == 1 ? g.my : j - 1, km = k == 1 ? g.mz : k - 1;
         const long long lxm = lin(g, im, j, k), lym = lin(g, i, jm, k), lzm = lin(g, i, j, km);
-        pex[t] = 0.5f * (ex[t] + ex[lxm]);
-        pey[t] = 0.5f * (ey[t] + ey[lym]);
-        pez[t] = 0.5f * (ez[t] + ez[lzm]);
-        pbx[t] = 0.5f * (bx[t] + bx[lym]);
-        pby[t] = 0.5f * (by[t] + by[lxm]);
-        pbz[t] = 0.5f * (0.5f * (bz[t] + bz[lxm]) + 0.5f * (bz[lym] + bz[lin(g, im, jm, k)]));
+        prim[2 * t] = make_float4(0.5f * (ex[t] + ex[lxm]), 0.5f * (ey[t] + ey[lym]), 0.5f * (ez[t] + ez[lzm]),
+                                  0.5f * (bx[t] + bx[lym]));
+        prim[2 * t + 1] = make_float4(0.5f * (by[t] + by[lxm]),
+                                      0.5f * (0.5f * (bz[t] + bz[lxm]) + 0.5f * (bz[lym] + bz[lin(g, im, jm, k)])),
+                                      0.0f, 0.0f);
     }
 }
 
-cudaError_t launch_primal(const Geom &g, float *const *f, float *const *pf, cudaStream_t st) {
-    k_primal<<<blocks_for(g.lot, 256), 256, 0, st>>>(g, f[0], f[1], f[2], f[3], f[4], f[5], pf[0], pf[1], pf[2],
-                                                     pf[3], pf[4], pf[5]);
+cudaError_t launch_primal(const Geom &g, float *const *f, float4 *prim, cudaStream_t st) {
+    k_primal<<<blocks_for(g.lot, 256), 256, 0, st>>>(g, f[0], f[1], f[2], f[3], f[4], f[5], prim);
     return cudaGetLastError();
 }
 

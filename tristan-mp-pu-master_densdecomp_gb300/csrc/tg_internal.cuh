@@ -184,7 +184,10 @@ __device__ __forceinline__ float sel(const float *a, int i) {
 // ---------------------------------------------------------------------------
 struct FieldPtrs {
     const float *ex, *ey, *ez, *bx, *by, *bz;          // staggered Yee (2D gather)
-    const float *pex, *pey, *pez, *pbx, *pby, *pbz;    // primal copies (3D gather)
+    // primal copies (3D gather), interleaved: cell t holds (pex, pey, pez,
+    // pbx) in prim[2t] and (pby, pbz, 0, 0) in prim[2t + 1], so a node's six
+    // components come in two 16-byte loads
+    const float4 *prim;
 };
 
 // ---------------------------------------------------------------------------
@@ -250,12 +253,13 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
 #pragma unroll
                 for (int r1 = 0; r1 < NS; r1++) {
                     const int l = row + r1;
-                    sx = sx + __ldg(f.pex + l) * axp[r1];
-                    sy = sy + __ldg(f.pey + l) * axp[r1];
-                    sz = sz + __ldg(f.pez + l) * axp[r1];
-                    sbx = sbx + __ldg(f.pbx + l) * axp[r1];
-                    sby = sby + __ldg(f.pby + l) * axp[r1];
-                    sbz = sbz + __ldg(f.pbz + l) * axp[r1];
+                    const float4 pa = __ldg(f.prim + 2 * l), pb = __ldg(f.prim + 2 * l + 1);
+                    sx = sx + pa.x * axp[r1];
+                    sy = sy + pa.y * axp[r1];
+                    sz = sz + pa.z * axp[r1];
+                    sbx = sbx + pa.w * axp[r1];
+                    sby = sby + pb.x * axp[r1];
+                    sbz = sbz + pb.y * axp[r1];
                 }
                 ex0 = ex0 + sx * ayp[r2] * az;
                 ey0 = ey0 + sy * ayp[r2] * az;
@@ -530,7 +534,7 @@ cudaError_t launch_fold(const Geom &g, const Params &P, float *const *cur, cudaS
 // kernel launches of one launch_fold
 int fold_launches(const Geom &g);
 cudaError_t launch_filter_pass(const Geom &g, float *const *in, float *const *out, cudaStream_t st);
-cudaError_t launch_primal(const Geom &g, float *const *f, float *const *pf, cudaStream_t st);
+cudaError_t launch_primal(const Geom &g, float *const *f, float4 *prim, cudaStream_t st);
 cudaError_t launch_fixed_to_float(const Geom &g, const Params &P, unsigned long long *const *fx, float *const *cur,
                                   cudaStream_t st);
 
