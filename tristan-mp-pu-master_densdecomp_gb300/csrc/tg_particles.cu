@@ -75,11 +75,22 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(int *hist, int *start, int 
     }
 }
 
+// The records are read in blocks of 32 x TG_SCATTER_STRIDE, transposed: the
+// lanes of a warp take records TG_SCATTER_STRIDE apart, and a warp's lanes
+// bound for one tile get consecutive slots there. A tile's consecutive
+// records, the lanes of one warp in the tile kernel, so come from different
+// cells even where a loader wrote each cell's particles side by side (the
+// window's shared atomics then meet fewer same-address and bank conflicts).
 __global__ void k_tile_scatter(Geom g, Species src, Species dst, const long long *count, const int *start,
                                int *cursor) {
+    constexpr int S = TG_SCATTER_STRIDE, B = 32 * S;
     const long long nmax = *count;
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nmax;
-         n += (long long)gridDim.x * blockDim.x) {
+    const long long mmax = (nmax + B - 1) / B * B;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < mmax;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(m % B);
+        const long long n = m - q + (q & 31) * S + (q >> 5);
+        if (n >= nmax) continue;
         const int cell = src.cell[n];
         if (cell < 0) continue;
         // the record is read before its slot is claimed, so the loads'

@@ -476,6 +476,11 @@ __device__ __forceinline__ void esirkepov(const Geom &g, float x2, float y2, flo
 // ---------------------------------------------------------------------------
 #define TG_WIN_BATCH 65536
 
+// read stride of the tile sorts' transposed record order (k_tile_scatter)
+#ifndef TG_SCATTER_STRIDE
+#define TG_SCATTER_STRIDE 8
+#endif
+
 __device__ __forceinline__ int wrap_i(int i, int lo, int n) {
     int r = (i - lo) % n;
     if (r < 0) r += n;
