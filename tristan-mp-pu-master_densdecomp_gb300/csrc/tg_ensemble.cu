@@ -219,11 +219,20 @@ __global__ void k_ens_count(const Geom *__restrict__ geoms, Species sp, const lo
 __global__ void k_ens_scatter(const Geom *__restrict__ geoms, Species src, Species dst,
                               const long long *__restrict__ bstart, int nbox, const int *__restrict__ tofs,
                               const int *start, int *cursor) {
+    // read order and early loads as in k_tile_scatter
+    constexpr int S = TG_SCATTER_STRIDE, B = 32 * S;
     const long long total = bstart[nbox];
-    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < total;
-         n += (long long)gridDim.x * blockDim.x) {
+    const long long mmax = (total + B - 1) / B * B;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < mmax;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(m % B);
+        const long long n = m - q + (q & 31) * S + (q >> 5);
+        if (n >= total) continue;
         const int cell = src.cell[n];
         if (cell < 0) continue;
+        const float ox = src.ox[n], oy = src.oy[n], oz = src.oz[n];
+        const float u = src.u[n], v = src.v[n], w = src.w[n], ch = src.ch[n];
+        const int32_t ind = src.ind[n], proc = src.proc[n], spl = src.splitlev[n];
         const int b = ens_box_of(bstart, nbox, n);
         const Geom &g = geoms[b];
         int i, j, k;
@@ -231,16 +240,16 @@ __global__ void k_ens_scatter(const Geom *__restrict__ geoms, Species src, Speci
         const int t = tofs[b] + tile_of(g, i, j, k);
         const long long d = (long long)start[t] + agg_inc(cursor, t);
         dst.cell[d] = cell;
-        dst.ox[d] = src.ox[n];
-        dst.oy[d] = src.oy[n];
-        dst.oz[d] = src.oz[n];
-        dst.u[d] = src.u[n];
-        dst.v[d] = src.v[n];
-        dst.w[d] = src.w[n];
-        dst.ch[d] = src.ch[n];
-        dst.ind[d] = src.ind[n];
-        dst.proc[d] = src.proc[n];
-        dst.splitlev[d] = src.splitlev[n];
+        dst.ox[d] = ox;
+        dst.oy[d] = oy;
+        dst.oz[d] = oz;
+        dst.u[d] = u;
+        dst.v[d] = v;
+        dst.w[d] = w;
+        dst.ch[d] = ch;
+        dst.ind[d] = ind;
+        dst.proc[d] = proc;
+        dst.splitlev[d] = spl;
     }
 }
 
