@@ -183,8 +183,9 @@ int tg_step(tg_ctx *ctx, int32_t nsteps);
    (each part grouped by tile), not in the order they went up. */
 int tg_step_host(tg_ctx *ctx, int32_t nsteps);
 /* Parts per species for the overlapped tg_step_host, 1..TG_HOST_PARTS_MAX;
-   0 (the default) picks by size: one part per 2^22 records of the larger
-   species, at most TG_HOST_PARTS_MAX. No counterpart in the reference. */
+   0 (the default) picks by size: about 512 records of the larger species
+   per tile and part, at most TG_HOST_PARTS_MAX. No counterpart in the
+   reference. */
 #define TG_HOST_PARTS_MAX 8
 int tg_set_host_parts(tg_ctx *ctx, int32_t parts);
 /* Page-lock the bound host arrays (the nine fields and 2 * maxhlf particle

@@ -817,7 +817,8 @@ extern "C" int tg_reorder(tg_ctx *ctx, int32_t lap, int32_t force) {
 // FP64 diagnostics
 // ---------------------------------------------------------------------------
 // pipe: the particles are grouped by tile part by part (a host-driven lap)
-static int run_diag(tg_ctx *ctx, bool particles, const HostPipe *pipe = nullptr) {
+// the diagnostics' launch descriptor over the particle buffers in use
+static DiagLaunch diag_launch(tg_ctx *ctx) {
     DiagLaunch d;
     memset(&d, 0, sizeof d);
     d.g = ctx->g;
@@ -826,14 +827,6 @@ static int run_diag(tg_ctx *ctx, bool particles, const HostPipe *pipe = nullptr)
         d.sp[s] = ctx->sp[ctx->par][s];
         d.tstart[s] = ctx->tstart[s];
         d.mass[s] = fabsf(ctx->P.qs[s] / ctx->P.qm[s]);
-    }
-    if (pipe && pipe->parts > 1) {
-        d.nparts = pipe->parts;
-        for (int h = 0; h < pipe->parts; h++)
-            for (int s = 0; s < 2; s++) {
-                d.psp[h][s] = species_at(ctx->sp[ctx->par][s], pipe->off[s][h]);
-                d.pts[h][s] = pipe->ts[s][h];
-            }
     }
     for (int a = 0; a < 6; a++) d.f[a] = ctx->f[a];
     d.rhofx = ctx->rhofx;
@@ -845,6 +838,13 @@ static int run_diag(tg_ctx *ctx, bool particles, const HostPipe *pipe = nullptr)
     d.counter = ctx->dcounter;
     d.ntimes = ctx->cfg.ntimes;
     d.status = ctx->d_status;
+    return d;
+}
+
+// the lap's diagnostics; particles = false when the particle pass already
+// ran (part by part inside a host-driven lap)
+static int run_diag(tg_ctx *ctx, bool particles) {
+    DiagLaunch d = diag_launch(ctx);
     d.particles = particles;
     CK(launch_diag(d, ctx->st));
     return TG_OK;
@@ -1143,6 +1143,16 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
                 CK(cudaMemcpyAsync(pipe->host + soff + (size_t)o * AOS, stg, (size_t)m * AOS,
                                    cudaMemcpyDeviceToHost, pipe->down));
                 k += 6;
+                if (ctx->cfg.diag_every > 0) {
+                    // the part's share of the diagnostics' particle pass, while
+                    // the part goes home and later parts arrive
+                    DiagLaunch d = diag_launch(ctx);
+                    d.sp[s] = dst;
+                    d.tstart[s] = ts;
+                    d.only = s + 1;
+                    CK(launch_diag_particles(d, st));
+                    k++;
+                }
             }
         }
         ctx->par = 1 - p0;
@@ -1212,9 +1222,9 @@ static int lap_kernels(tg_ctx *ctx, bool sort_now, int *nk, int li = 0, const Ho
     }
     if (ctx->cfg.diag_every > 0) {
         CK(mark(ctx, li, 7, 0));
-        int rr = run_diag(ctx, true, pipe);
+        int rr = run_diag(ctx, !pipe);
         if (rr) return rr;
-        k += 4 + ctx->cfg.ntimes + (pipe ? pipe->parts - 1 : 0);
+        k += 3 + ctx->cfg.ntimes + (pipe ? 0 : 1);
         CK(mark(ctx, li, 7, 1));
     }
     *nk = k;
@@ -1338,11 +1348,15 @@ static int host_lap(tg_ctx *ctx) {
     cudaStream_t st = ctx->st;
     const size_t lot = (size_t)g.lot;
     CK(cudaStreamSynchronize(st));
-    // parts per species: as set, else one per 2^22 records of the larger species
+    // parts per species: as set, else about 512 records of the larger
+    // species per tile and part (measured best on the 2D and 3D benchmark
+    // plasmas: every part's tile launch clears and flushes every tile's
+    // window, so smaller parts pay that per-tile cost more often, larger
+    // ones overlap less of the transfers)
     int parts = ctx->host_parts;
     if (parts == 0) {
         const long long big = n[0] > n[1] ? n[0] : n[1];
-        parts = (int)(big >> 22);
+        parts = (int)((big + 256LL * g.ntiles) / (512LL * g.ntiles));
         parts = parts < 1 ? 1 : parts > TG_HOST_PARTS_MAX ? TG_HOST_PARTS_MAX : parts;
     }
     pipe.parts = parts;

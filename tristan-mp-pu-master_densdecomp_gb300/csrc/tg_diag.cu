@@ -38,6 +38,7 @@ struct DiagArgs {
     double *acc;                // [D_N]
     float mass[2];              // |q/qm| per species
     int *status;
+    int only;                   // 0 both species, 1 ions only, 2 electrons only
 };
 
 #ifndef TG_DIAG_MINB
@@ -58,9 +59,11 @@ __global__ void __launch_bounds__(256, TG_DIAG_MINB) k_diag_particles(DiagArgs a
     double part[5] = {0, 0, 0, 0, 0};  // eki, eke, px, py, pz
     // the window is exact for up to 65536 contributions per node: a denser
     // tile deposits straight to global memory
-    const bool use_win = (a.tstart[0][tile + 1] - a.tstart[0][tile]) + (a.tstart[1][tile + 1] - a.tstart[1][tile]) <=
-                         TG_WIN_BATCH;
-    for (int s = 0; s < 2; s++) {
+    const int s0 = a.only == 2 ? 1 : 0, s1 = a.only == 1 ? 1 : 2;
+    int nt = 0;
+    for (int s = s0; s < s1; s++) nt += a.tstart[s][tile + 1] - a.tstart[s][tile];
+    const bool use_win = nt <= TG_WIN_BATCH;
+    for (int s = s0; s < s1; s++) {
         const Species sp = a.sp[s];
         const int beg = a.tstart[s][tile], end = a.tstart[s][tile + 1];
         const float qs = a.P.qs[s], m = a.mass[s];
@@ -673,7 +676,7 @@ static int dgrid(long long n) {
     return (int)b;
 }
 
-cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
+cudaError_t launch_diag_particles(const DiagLaunch &d, cudaStream_t st) {
     const Geom &g = d.g;
     DiagArgs a;
     a.g = g;
@@ -686,6 +689,7 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
     a.rhofx = d.rhofx;
     a.acc = d.acc;
     a.status = d.status;
+    a.only = d.only;
     const size_t smem = (size_t)g.wcells * 8;
     cudaError_t e = cudaSuccess;
 #define TG_DL(D, O)                                                                                     \
@@ -695,21 +699,20 @@ cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
         if (e != cudaSuccess) return e;                                                                 \
         k_diag_particles<D, O><<<g.ntiles, 256, smem, st>>>(a);                                         \
     } while (0)
-    for (int h = 0; h < (d.nparts > 0 ? d.nparts : 1); h++) {
-        if (d.nparts > 0)
-            for (int s = 0; s < 2; s++) {
-                a.sp[s] = d.psp[h][s];
-                a.tstart[s] = d.pts[h][s];
-            }
-        if (!d.particles) {
-        } else if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
-        else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
-        else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
-        else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);
-        else if (g.dims == 3 && g.order == 2) TG_DL(3, 2);
-        else TG_DL(3, 3);
-    }
+    if (g.dims == 2 && g.order == 1) TG_DL(2, 1);
+    else if (g.dims == 2 && g.order == 2) TG_DL(2, 2);
+    else if (g.dims == 2 && g.order == 3) TG_DL(2, 3);
+    else if (g.dims == 3 && g.order == 1) TG_DL(3, 1);
+    else if (g.dims == 3 && g.order == 2) TG_DL(3, 2);
+    else TG_DL(3, 3);
 #undef TG_DL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st) {
+    const Geom &g = d.g;
+    cudaError_t e = cudaSuccess;
+    if (d.particles && (e = launch_diag_particles(d, st)) != cudaSuccess) return e;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int nx = g.mx - g.ng, ny = g.my - g.ng, nz = g.dims == 3 ? g.mz - g.ngz : 1;
     const long long n = (long long)nx * ny * nz;

@@ -175,31 +175,38 @@ __global__ void __launch_bounds__(256) k_filter(Geom g, const float *__restrict_
 // every input element is read from HBM about once per pass instead of 27
 // times through the cache. The plane k+2 is loaded into registers before
 // plane k is filtered and stored into the ring after it, so its memory
-// latency overlaps the stencil work. Each cell then runs the same selection
-// and the same stencil27 as filter_one.
-#define TG_F3_TX 32
+// latency overlaps the stencil work. Each thread filters two neighbouring
+// x cells: a row's four values come in two 8-byte shared loads and serve
+// both cells' stencils (the 27 terms of each cell three times fewer shared
+// loads than one cell per thread); each cell runs the same selection and
+// the same stencil27 as filter_one.
+#define TG_F3_CX 32  // cells per CTA along x (two per thread)
+#define TG_F3_NX 16  // threads per CTA along x
 #define TG_F3_TY 8
 #define TG_F3_KC 32
-#define TG_F3_SX (TG_F3_TX + 2)
+#define TG_F3_NT (TG_F3_NX * TG_F3_TY)
+#define TG_F3_SX (TG_F3_CX + 2)
 #define TG_F3_SY (TG_F3_TY + 2)
-#define TG_F3_PER ((TG_F3_SX * TG_F3_SY + TG_F3_TX * TG_F3_TY - 1) / (TG_F3_TX * TG_F3_TY))  // halo cells per thread
-__global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
+#define TG_F3_PER ((TG_F3_SX * TG_F3_SY + TG_F3_NT - 1) / TG_F3_NT)  // halo cells per thread
+__global__ void __launch_bounds__(TG_F3_NT)
     k_filter3d(Geom g, const float *__restrict__ i0, const float *__restrict__ i1, const float *__restrict__ i2,
                float *o0, float *o1, float *o2) {
     constexpr int SX = TG_F3_SX, SY = TG_F3_SY, PER = TG_F3_PER;
-    __shared__ float sm[3][3][SY][SX];  // [component][plane ring][y][x]
+    // [component][plane ring][y][x]; rows of 34 floats keep every even x
+    // 8-byte aligned
+    __shared__ __align__(16) float sm[3][3][SY][SX];
     const RefreshMap Rx{g.mx, g.ng, g.per[0]}, Ry{g.my, g.ng, g.per[1]}, Rz{g.mz, g.ngz, g.per[2]};
-    const int ib = blockIdx.x * TG_F3_TX + 1, jb = blockIdx.y * TG_F3_TY + 1;
+    const int ib = blockIdx.x * TG_F3_CX + 1, jb = blockIdx.y * TG_F3_TY + 1;
     const int kb = blockIdx.z * TG_F3_KC + 1;
     const int ke = min(kb + TG_F3_KC, g.mz + 1);
-    const int tid = threadIdx.y * TG_F3_TX + threadIdx.x;
+    const int tid = threadIdx.y * TG_F3_NX + threadIdx.x;
     // this thread's halo cells of a plane: their (refreshed) x-y offset, or
     // -1 outside the array; each plane adds its (refreshed) z offset
     long long xy[PER];
     int slot_xy[PER];
 #pragma unroll
     for (int e = 0; e < PER; e++) {
-        const int t = tid + e * TG_F3_TX * TG_F3_TY;
+        const int t = tid + e * TG_F3_NT;
         slot_xy[e] = t < SX * SY ? t : -1;
         xy[e] = -1;
         if (t < SX * SY) {
@@ -232,8 +239,8 @@ __global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
     const int ilo = g.ng / 2 + 1, ihi = g.mx - (g.ng / 2 + 1);
     const int jlo = g.ng / 2 + 1, jhi = g.my - (g.ng / 2 + 1);
     const int klo = g.ngz / 2 + 1, khi = g.mz - (g.ngz / 2 + 1);
-    const int i = ib + threadIdx.x, j = jb + threadIdx.y;
-    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+    const int ia = ib + 2 * threadIdx.x, j = jb + threadIdx.y;  // cells ia and ia + 1
+    const int lx = 2 * threadIdx.x, ly = threadIdx.y + 1;       // slot of x = ia - 1
     fetch(kb - 1);
     put(kb - 1);
     fetch(kb);
@@ -243,28 +250,42 @@ __global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
     __syncthreads();
     for (int k = kb; k < ke; k++) {
         if (k + 1 < ke) fetch(k + 2);  // in flight while plane k is filtered
-        if (i <= g.mx && j <= g.my) {
-            const bool in_ik = i >= ilo && i <= ihi && k >= klo && k <= khi;
-            const bool in_xy = in_ik && j >= jlo && j <= jhi;
-            const bool in_z = in_ik && j >= jlo && j <= jhi + 2;
-            const int s0 = (k + 2) % 3, s1 = k % 3, s2 = (k + 1) % 3;
-            float res[3];
+        if (ia <= g.mx && j <= g.my) {
+            const bool kin = k >= klo && k <= khi;
+            const bool jxy = j >= jlo && j <= jhi, jz = j >= jlo && j <= jhi + 2;
+            const bool ina = kin && ia >= ilo && ia <= ihi, inb = kin && ia + 1 >= ilo && ia + 1 <= ihi;
+            const int sl[3] = {(k + 2) % 3, k % 3, (k + 1) % 3};
+            float ra[3], rb[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                const bool st = c == 2 ? in_z : in_xy;
-                if (!st) {
-                    res[c] = sm[c][s1][ly][lx];
-                } else {
-                    res[c] = stencil27([&](int di, int dj, int dk) {
-                        const int sl = dk < 0 ? s0 : dk > 0 ? s2 : s1;
-                        return sm[c][sl][ly + dj][lx + di];
-                    });
-                }
+                const bool jc = c == 2 ? jz : jxy;
+                // rows (dj, dk): x = ia - 1 .. ia + 2
+                float r[3][3][4];
+#pragma unroll
+                for (int dk = 0; dk < 3; dk++)
+#pragma unroll
+                    for (int dj = 0; dj < 3; dj++) {
+                        const float2 p = *reinterpret_cast<const float2 *>(&sm[c][sl[dk]][ly + dj - 1][lx]);
+                        const float2 q = *reinterpret_cast<const float2 *>(&sm[c][sl[dk]][ly + dj - 1][lx + 2]);
+                        r[dk][dj][0] = p.x;
+                        r[dk][dj][1] = p.y;
+                        r[dk][dj][2] = q.x;
+                        r[dk][dj][3] = q.y;
+                    }
+                ra[c] = (jc && ina) ? stencil27([&](int di, int dj, int dk) { return r[dk + 1][dj + 1][di + 1]; })
+                                    : r[1][1][1];
+                rb[c] = (jc && inb) ? stencil27([&](int di, int dj, int dk) { return r[dk + 1][dj + 1][di + 2]; })
+                                    : r[1][1][2];
             }
-            const long long t = lin(g, i, j, k);
-            o0[t] = res[0];
-            o1[t] = res[1];
-            o2[t] = res[2];
+            const long long t = lin(g, ia, j, k);
+            o0[t] = ra[0];
+            o1[t] = ra[1];
+            o2[t] = ra[2];
+            if (ia + 1 <= g.mx) {
+                o0[t + 1] = rb[0];
+                o1[t + 1] = rb[1];
+                o2[t + 1] = rb[2];
+            }
         }
         __syncthreads();  // plane k-1's slot is free
         if (k + 1 < ke) {
@@ -276,9 +297,9 @@ __global__ void __launch_bounds__(TG_F3_TX *TG_F3_TY)
 
 cudaError_t launch_filter_pass(const Geom &g, float *const *in, float *const *out, cudaStream_t st) {
     if (g.dims == 3) {
-        const dim3 grid((g.mx + TG_F3_TX - 1) / TG_F3_TX, (g.my + TG_F3_TY - 1) / TG_F3_TY,
+        const dim3 grid((g.mx + TG_F3_CX - 1) / TG_F3_CX, (g.my + TG_F3_TY - 1) / TG_F3_TY,
                         (g.mz + TG_F3_KC - 1) / TG_F3_KC);
-        k_filter3d<<<grid, dim3(TG_F3_TX, TG_F3_TY), 0, st>>>(g, in[0], in[1], in[2], out[0], out[1], out[2]);
+        k_filter3d<<<grid, dim3(TG_F3_NX, TG_F3_TY), 0, st>>>(g, in[0], in[1], in[2], out[0], out[1], out[2]);
     } else {
         k_filter<2><<<blocks_for(g.lot, 256), 256, 0, st>>>(g, in[0], in[1], in[2], out[0], out[1], out[2]);
     }

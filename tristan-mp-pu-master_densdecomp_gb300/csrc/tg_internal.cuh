@@ -467,14 +467,14 @@ struct DiagLaunch {
     unsigned long long *counter;
     int ntimes;
     int *status;
-    bool particles;  // false: the lap's tile kernel already summed the particles
-    // nparts > 0: the particles are grouped by tile part by part (a
-    // host-driven lap); the particle pass runs once per part
-    int nparts;
-    Species psp[TG_HOST_PARTS_MAX][2];
-    const int *pts[TG_HOST_PARTS_MAX][2];
+    bool particles;  // false: the particle pass already ran (part by part in a host-driven lap)
+    int only;        // particle pass: 0 both species, 1 the ions only, 2 the electrons only
 };
+// the whole lap's diagnostics: particle pass (when d.particles), the
+// charge's filter passes, the field reductions and the history record
 cudaError_t launch_diag(const DiagLaunch &d, cudaStream_t st);
+// the particle pass alone over d.sp / d.tstart (d.only selects the species)
+cudaError_t launch_diag_particles(const DiagLaunch &d, cudaStream_t st);
 // flow-frame spectra (save_spectrum_2d): the gamma range (two float bit
 // patterns, seeded with 1.0), then per species slice means and the histogram
 struct SpecGrid;
