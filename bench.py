@@ -255,12 +255,15 @@ def run_e2e(cfg, ions, lecs, e2e_steps, host_parts, device):
     huge = sim.host_huge_fraction()
     # one tg_step_host call per lap: E, B and the records up, the lap,
     # everything back, as the reference's main loop would drive it
+    laps = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         sim.step_host(1)
+        laps.append((time.perf_counter() - t1) * 1e3)
     dt = time.perf_counter() - t0
     sim.close()
-    return dt, h2d, d2h, huge
+    return dt, h2d, d2h, huge, laps
 
 
 def copy_only_ms(h2d, d2h, device, reps=3):
@@ -379,7 +382,7 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
         ms_f = allreduce_max(ms_f, ws, args.impl)
         fixed = {"value": ws * n_p * steps / (ms_f / 1e3), "ms_per_step": ms_f / steps,
                  "particle_kernel_ms": ph_f["particles"], "deposit": DEPOSIT_FIXED}
-    dt_e2e, h2d, d2h, huge_lap = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
+    dt_e2e, h2d, d2h, huge_lap, lap_ms = run_e2e(cfg, ions, lecs, e2e_steps, args.host_parts, device)
     ms_e2e = dt_e2e / e2e_steps * 1e3
     ms_link, huge_link = copy_only_ms(h2d, d2h, device)
     e2e = {"value": ws * n_p * e2e_steps / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -397,7 +400,9 @@ def measure_workload(name, args, ws, rank, local, steps, warmup, e2e_steps, cpu_
            "mode": "one tg_step_host call per lap: E, B, particle records up; the lap; fields, "
                    "records, counts down (each species in parts: a part is sorted and pushed as soon "
                    "as it is in, and goes home while later parts arrive)",
-           "host_parts": args.host_parts or "by size"}
+           "host_parts": args.host_parts or "by size",
+           # each lap's host wall-clock (the value above is their mean)
+           "lap_ms": [round(v, 3) for v in lap_ms], "lap_ms_median": statistics.median(lap_ms)}
     peak, peak_kind = measured_peak_hbm()
     t_kernel = phases["particles"] / 1e3
     alg = tile_kernel_bytes(cfg, n_p, False)
