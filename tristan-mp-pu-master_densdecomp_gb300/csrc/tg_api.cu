@@ -241,7 +241,7 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.wy = ty + g.wlo + g.whi;
     g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
     g.wcells = g.wx * g.wy * g.wz;
-    const size_t smem = (size_t)6 * g.wcells * 4;  // two 32-bit words per cell, 3 components
+    const size_t smem = tile_smem_bytes(c.dims, g.wcells);  // window (and the 2D field copy)
     if (smem > 227 * 1024)
         return geom_fail(err, errlen, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
     return TG_OK;

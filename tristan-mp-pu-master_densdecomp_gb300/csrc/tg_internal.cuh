@@ -28,6 +28,13 @@ namespace tg {
 #define TG_SIXTH 0x1.555556p-3f     // 1/6
 #define TG_NEGSIXTH (-0x1.555556p-3f)
 
+// dynamic shared memory of a tile kernel: the deposit window (two 32-bit
+// words per cell, three components) and, in 2D, the tile's copy of the six
+// field arrays over the same cells
+__host__ __device__ inline size_t tile_smem_bytes(int dims, int wcells) {
+    return (size_t)6 * wcells * 4 * (dims == 2 ? 2 : 1);
+}
+
 // device status bits
 enum : int32_t { ST_BOUNDS = 1, ST_NAN = 2, ST_OVERFLOW = 4, ST_WINDOW = 8, ST_CHARGE_GRID = 16 };
 
@@ -190,6 +197,15 @@ struct FieldPtrs {
     const float4 *prim;
 };
 
+// A tile's copy of the six staggered 2D field arrays in shared memory
+// ([6][h][w]: ex, ey, ez, bx, by, bz) over nodes x0 .. x0 + w - 1,
+// y0 .. y0 + h - 1 (1-based), read by the gather of every particle whose
+// nodes lie inside it
+struct FieldWin {
+    const float *s;
+    int x0, y0, w, h;
+};
+
 // ---------------------------------------------------------------------------
 // Mover: shape-consistent gather + Boris + position advance, in absolute
 // coordinates (mover_{1,2,3}ord, code/particles_movedeposit.F90:356-1271).
@@ -198,7 +214,8 @@ struct FieldPtrs {
 // ---------------------------------------------------------------------------
 template <int DIM, int ORDER>
 __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f, const Params &P, float qm,
-                                              float &x, float &y, float &z, float &u, float &v, float &w) {
+                                              float &x, float &y, float &z, float &u, float &v, float &w,
+                                              const FieldWin *win = nullptr) {
     constexpr int NS = ShapeN<ORDER>::NS;
     const float c = P.c;
     const float cinv = 1.0f / c;
@@ -267,6 +284,30 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
                 bx0 = bx0 + sbx * ayp[r2] * az;
                 by0 = by0 + sby * ayp[r2] * az;
                 bz0 = bz0 + sbz * ayp[r2] * az;
+            }
+        }
+    } else if (win && id - 3 + bxd >= win->x0 && ip - 4 + bxd + NS < win->x0 + win->w &&
+               jd - 3 + byd >= win->y0 && jp - 4 + byd + NS < win->y0 + win->h) {
+        // every node in the tile's shared copy: the same loop on shared loads
+        const int plane = win->w * win->h;
+        const float *sex = win->s, *sey = sex + plane, *sez = sey + plane;
+        const float *sbx = sez + plane, *sby = sbx + plane, *sbz = sby + plane;
+#pragma unroll 1
+        for (int r2 = 0; r2 < NS; r2++) {
+            const int rowp = win->w * (jp - 3 + byd + r2 - win->y0);
+            const int rowd = win->w * (jd - 3 + byd + r2 - win->y0);
+            const float ay = sel<NS>(ayp, r2), wy = sel<NS>(wyd, r2);
+#pragma unroll
+            for (int r1 = 0; r1 < NS; r1++) {
+                const int colp = ip - 3 + bxd + r1 - win->x0;
+                const int cold = id - 3 + bxd + r1 - win->x0;
+                const int lpp = colp + rowp, lpd = colp + rowd, ldp = cold + rowp, ldd = cold + rowd;
+                ex0 = ex0 + sex[ldp] * wxd[r1] * ay;
+                ey0 = ey0 + sey[lpd] * axp[r1] * wy;
+                ez0 = ez0 + sez[lpp] * axp[r1] * ay;
+                bx0 = bx0 + sbx[lpd] * axp[r1] * wy;
+                by0 = by0 + sby[ldp] * wxd[r1] * ay;
+                bz0 = bz0 + sbz[ldd] * wxd[r1] * wy;
             }
         }
     } else {

@@ -609,7 +609,8 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
 // its new tile.
 template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
 __device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXED> &sink, const Species &sp, int n,
-                                              int *newcount, float qm, float qs, double walloc, double x2in) {
+                                              int *newcount, float qm, float qs, double walloc, double x2in,
+                                              const FieldWin *win = nullptr) {
     const Geom &g = a.g;
             if (sp.cell[n] < 0) return;  // discarded since the last sort
             float x, y, z;
@@ -621,7 +622,7 @@ __device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXE
                     sp.cell[n] = -1;
                     return;
                 }
-                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w);
+                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w, win);
                 if (DIM == 2 && DEPOSIT && (double)(x + (float)a.P.mxcum) < walloc &&
                     !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
                                   y, z, u, v, w)) {
@@ -689,6 +690,26 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     sink.g = &a.g;
     sink.status = a.status;
     const int nwords = 6 * g.wcells;
+    // 2D: the tile's copy of the six field arrays over the window's cells,
+    // behind the window (every particle whose gather nodes lie inside reads
+    // them from shared memory)
+    FieldWin fwin;
+    fwin.s = reinterpret_cast<const float *>(smem_raw) + nwords;
+    fwin.x0 = sink.wx0;
+    fwin.y0 = sink.wy0;
+    fwin.w = g.wx;
+    fwin.h = g.wy;
+    if (DIM == 2 && PUSH) {
+        float *fs = reinterpret_cast<float *>(smem_raw) + nwords;
+        const float *src[6] = {a.f.ex, a.f.ey, a.f.ez, a.f.bx, a.f.by, a.f.bz};
+#pragma unroll
+        for (int comp = 0; comp < 6; comp++)
+            for (int c = threadIdx.x; c < g.wcells; c += blockDim.x) {
+                const int i = fwin.x0 + c % g.wx, j = fwin.y0 + c / g.wx;
+                fs[comp * g.wcells + c] =
+                    (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) ? __ldg(src[comp] + (i - 1) + g.sy * (j - 1)) : 0.0f;
+            }
+    }
     if (DEPOSIT) {
         for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
         __syncthreads();
@@ -716,7 +737,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
             const int b1 = min(end, b0 + (batch - since));
 #pragma unroll 1
             for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x)
-                particle_step<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, sink, sp, n, a.newcount[s], qm, qs, walloc, x2in);
+                particle_step<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, sink, sp, n, a.newcount[s], qm, qs, walloc, x2in,
+                                                                 DIM == 2 ? &fwin : nullptr);
             since += b1 - b0;
             b0 = b1;
             if (DEPOSIT && since == batch) {
