@@ -241,7 +241,20 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     g.wy = ty + g.wlo + g.whi;
     g.wz = c.dims == 3 ? tz + g.wlo + g.whi : 1;
     g.wcells = g.wx * g.wy * g.wz;
-    const size_t smem = tile_smem_bytes(c.dims, g.wcells);  // window (and the 2D field copy)
+    // 3D field copy over the gather's reach (nodes [i - 1, i + 2] of a
+    // particle starting in cell i, widened by the drift), kept only while two
+    // CTAs per SM fit beside the deposit window
+    g.fw_lo = g.fwx = g.fwy = g.fwz = g.fwcells = 0;
+    if (c.dims == 3) {
+        const int drift_cells = g.wlo - (c.order == 1 ? 1 : 2);
+        g.fw_lo = drift_cells + 1;
+        g.fwx = tx + 2 * drift_cells + 3;
+        g.fwy = ty + 2 * drift_cells + 3;
+        g.fwz = tz + 2 * drift_cells + 3;
+        g.fwcells = g.fwx * g.fwy * g.fwz;
+        if (tile_smem_bytes(3, g.wcells, g.fwcells) > 112 * 1024) g.fw_lo = g.fwx = g.fwy = g.fwz = g.fwcells = 0;
+    }
+    const size_t smem = tile_smem_bytes(c.dims, g.wcells, g.fwcells);  // window and field copy
     if (smem > 227 * 1024)
         return geom_fail(err, errlen, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
     return TG_OK;

@@ -508,7 +508,7 @@ extern "C" int tg_ens_init(const tg_config *cfgs, int32_t nbox, tg_ens **out) {
     E->ncell = fo;
     E->T = to;
     E->capacity = cap;
-    E->smem = tile_smem_bytes(2, maxw);
+    E->smem = tile_smem_bytes(2, maxw, 0);
     if (cap >= (1LL << 31)) {
         delete E;
         return efail(nullptr, TG_ERR_ARG, "tg_ens_init: %lld particles per species exceed int32 indices", cap);

@@ -29,10 +29,14 @@ namespace tg {
 #define TG_NEGSIXTH (-0x1.555556p-3f)
 
 // dynamic shared memory of a tile kernel: the deposit window (two 32-bit
-// words per cell, three components) and, in 2D, the tile's copy of the six
-// field arrays over the same cells
-__host__ __device__ inline size_t tile_smem_bytes(int dims, int wcells) {
-    return (size_t)6 * wcells * 4 * (dims == 2 ? 2 : 1);
+// words per cell, three components) and the tile's field copy: in 2D the
+// six field arrays over the window's cells, in 3D the interleaved primal
+// copies (32 B per cell) over the gather's reach, 16-byte aligned
+__host__ __device__ inline size_t tile_window_bytes(int wcells) { return (size_t)6 * wcells * 4; }
+__host__ __device__ inline size_t tile_fieldwin_offset(int wcells) { return (tile_window_bytes(wcells) + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t tile_smem_bytes(int dims, int wcells, int fwcells) {
+    if (dims == 2) return 2 * tile_window_bytes(wcells);
+    return fwcells > 0 ? tile_fieldwin_offset(wcells) + (size_t)32 * fwcells : tile_window_bytes(wcells);
 }
 
 // device status bits
@@ -59,6 +63,10 @@ struct Geom {
     int wlo, whi;  // halo below / above the tile, same on every axis
     int wx, wy, wz;
     int wcells;
+    // 3D: the tile's copy of the interleaved primal fields over the gather's
+    // reach (fw_lo cells below the tile, fwx x fwy x fwz cells), when two
+    // CTAs per SM still fit beside the deposit window (fwcells = 0: none)
+    int fw_lo, fwx, fwy, fwz, fwcells;
 };
 
 // particle storage: structure of arrays, cell index + in-cell offset
@@ -206,6 +214,13 @@ struct FieldWin {
     int x0, y0, w, h;
 };
 
+// A 3D tile's copy of the interleaved primal fields (FieldPtrs::prim) in
+// shared memory, two float4 per cell, over nodes x0 .. x0 + w - 1 (and y, z)
+struct FieldWin3 {
+    const float4 *s;
+    int x0, y0, z0, w, h, d;
+};
+
 // ---------------------------------------------------------------------------
 // Mover: shape-consistent gather + Boris + position advance, in absolute
 // coordinates (mover_{1,2,3}ord, code/particles_movedeposit.F90:356-1271).
@@ -215,7 +230,7 @@ struct FieldWin {
 template <int DIM, int ORDER>
 __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f, const Params &P, float qm,
                                               float &x, float &y, float &z, float &u, float &v, float &w,
-                                              const FieldWin *win = nullptr) {
+                                              const FieldWin *win = nullptr, const FieldWin3 *win3 = nullptr) {
     constexpr int NS = ShapeN<ORDER>::NS;
     const float c = P.c;
     const float cinv = 1.0f / c;
@@ -257,7 +272,39 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
         }
     }
     float ex0 = 0.0f, ey0 = 0.0f, ez0 = 0.0f, bx0 = 0.0f, by0 = 0.0f, bz0 = 0.0f;
-    if (DIM == 3) {
+    if (DIM == 3 && win3 && ip - 3 + bxd >= win3->x0 && ip - 4 + bxd + NS < win3->x0 + win3->w &&
+        jp - 3 + byd >= win3->y0 && jp - 4 + byd + NS < win3->y0 + win3->h && kp - 3 + bzd >= win3->z0 &&
+        kp - 4 + bzd + NS < win3->z0 + win3->d) {
+        // every node in the tile's shared copy: the same loop on shared loads
+        const int sy = win3->w, sz = win3->w * win3->h;
+#pragma unroll 1
+        for (int r3 = 0; r3 < NS; r3++) {
+            const float az = sel<NS>(azp, r3);
+#pragma unroll
+            for (int r2 = 0; r2 < NS; r2++) {
+                const int row = (ip - 3 + bxd - win3->x0) + sy * (jp - 3 + byd + r2 - win3->y0) +
+                                sz * (kp - 3 + bzd + r3 - win3->z0);
+                float sx = 0.0f, sy_ = 0.0f, sz_ = 0.0f, sbx = 0.0f, sby = 0.0f, sbz = 0.0f;
+#pragma unroll
+                for (int r1 = 0; r1 < NS; r1++) {
+                    const int l = row + r1;
+                    const float4 pa = win3->s[2 * l], pb = win3->s[2 * l + 1];
+                    sx = sx + pa.x * axp[r1];
+                    sy_ = sy_ + pa.y * axp[r1];
+                    sz_ = sz_ + pa.z * axp[r1];
+                    sbx = sbx + pa.w * axp[r1];
+                    sby = sby + pb.x * axp[r1];
+                    sbz = sbz + pb.y * axp[r1];
+                }
+                ex0 = ex0 + sx * ayp[r2] * az;
+                ey0 = ey0 + sy_ * ayp[r2] * az;
+                ez0 = ez0 + sz_ * ayp[r2] * az;
+                bx0 = bx0 + sbx * ayp[r2] * az;
+                by0 = by0 + sby * ayp[r2] * az;
+                bz0 = bz0 + sbz * ayp[r2] * az;
+            }
+        }
+    } else if (DIM == 3) {
         // planes rolled (code size), rows and columns unrolled
 #pragma unroll 1
         for (int r3 = 0; r3 < NS; r3++) {

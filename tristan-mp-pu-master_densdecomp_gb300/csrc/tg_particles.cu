@@ -231,7 +231,7 @@ static int grid_for(long long n, int block) {
 }
 
 cudaError_t launch_tiles(const TileArgs &a, bool fixed, bool push, bool deposit, cudaStream_t st) {
-    const size_t smem = deposit ? tile_smem_bytes(a.g.dims, a.g.wcells) : 0;
+    const size_t smem = deposit ? tile_smem_bytes(a.g.dims, a.g.wcells, a.g.fwcells) : 0;
     const int d = a.g.dims, o = a.g.order;
     if (d == 2 && o == 1) return launch_tiles_o<2, 1>(a, fixed, push, deposit, st, smem);
     if (d == 2 && o == 2) return launch_tiles_o<2, 2>(a, fixed, push, deposit, st, smem);

@@ -610,7 +610,7 @@ __device__ __forceinline__ void flush_window(const TileArgs &a, const WindowSink
 template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
 __device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXED> &sink, const Species &sp, int n,
                                               int *newcount, float qm, float qs, double walloc, double x2in,
-                                              const FieldWin *win = nullptr) {
+                                              const FieldWin *win = nullptr, const FieldWin3 *win3 = nullptr) {
     const Geom &g = a.g;
             if (sp.cell[n] < 0) return;  // discarded since the last sort
             float x, y, z;
@@ -622,7 +622,7 @@ __device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXE
                     sp.cell[n] = -1;
                     return;
                 }
-                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w, win);
+                push_particle<DIM, ORDER>(g, a.f, a.P, qm, x, y, z, u, v, w, win, win3);
                 if (DIM == 2 && DEPOSIT && (double)(x + (float)a.P.mxcum) < walloc &&
                     !wall_reflect(sink, a.P.c, a.gammawall, a.betawall, walloc, a.P.mxcum, sp.ch[n] * qs, x,
                                   y, z, u, v, w)) {
@@ -710,6 +710,29 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                     (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) ? __ldg(src[comp] + (i - 1) + g.sy * (j - 1)) : 0.0f;
             }
     }
+    // 3D: the interleaved primal copies over the gather's reach
+    FieldWin3 fwin3;
+    fwin3.s = reinterpret_cast<const float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+    fwin3.x0 = g.ox + tix * g.tx - g.fw_lo;
+    fwin3.y0 = g.oy + tiy * g.ty - g.fw_lo;
+    fwin3.z0 = g.oz + tiz * g.tz - g.fw_lo;
+    fwin3.w = g.fwx;
+    fwin3.h = g.fwy;
+    fwin3.d = g.fwz;
+    if (DIM == 3 && PUSH && g.fwcells > 0) {
+        float4 *fs = reinterpret_cast<float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+        for (int c = threadIdx.x; c < g.fwcells; c += blockDim.x) {
+            const int i = fwin3.x0 + c % g.fwx, j = fwin3.y0 + (c / g.fwx) % g.fwy, k = fwin3.z0 + c / (g.fwx * g.fwy);
+            float4 pa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), pb = pa;
+            if (i >= 1 && i <= g.mx && j >= 1 && j <= g.my && k >= 1 && k <= g.mz) {
+                const long long l = lin(g, i, j, k);
+                pa = __ldg(a.f.prim + 2 * l);
+                pb = __ldg(a.f.prim + 2 * l + 1);
+            }
+            fs[2 * c] = pa;
+            fs[2 * c + 1] = pb;
+        }
+    }
     if (DEPOSIT) {
         for (int t = threadIdx.x; t < nwords; t += blockDim.x) winlo[t] = 0u;
         __syncthreads();
@@ -738,7 +761,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
 #pragma unroll 1
             for (int n = b0 + threadIdx.x; n < b1; n += blockDim.x)
                 particle_step<DIM, ORDER, FIXED, PUSH, DEPOSIT>(a, sink, sp, n, a.newcount[s], qm, qs, walloc, x2in,
-                                                                 DIM == 2 ? &fwin : nullptr);
+                                                                 DIM == 2 ? &fwin : nullptr,
+                                                                 DIM == 3 && g.fwcells > 0 ? &fwin3 : nullptr);
             since += b1 - b0;
             b0 = b1;
             if (DEPOSIT && since == batch) {
