@@ -30,13 +30,14 @@ namespace tg {
 
 // dynamic shared memory of a tile kernel: the deposit window (two 32-bit
 // words per cell, three components) and the tile's field copy: in 2D the
-// six field arrays over the window's cells, in 3D the interleaved primal
-// copies (32 B per cell) over the gather's reach, 16-byte aligned
+// six field arrays over the window's cells, in 3D the primal copies (24 B
+// per cell: a float4 and a float2 array) over the gather's reach, 16-byte
+// aligned
 __host__ __device__ inline size_t tile_window_bytes(int wcells) { return (size_t)6 * wcells * 4; }
 __host__ __device__ inline size_t tile_fieldwin_offset(int wcells) { return (tile_window_bytes(wcells) + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t tile_smem_bytes(int dims, int wcells, int fwcells) {
     if (dims == 2) return 2 * tile_window_bytes(wcells);
-    return fwcells > 0 ? tile_fieldwin_offset(wcells) + (size_t)32 * fwcells : tile_window_bytes(wcells);
+    return fwcells > 0 ? tile_fieldwin_offset(wcells) + (size_t)24 * fwcells : tile_window_bytes(wcells);
 }
 
 // device status bits
@@ -214,10 +215,14 @@ struct FieldWin {
     int x0, y0, w, h;
 };
 
-// A 3D tile's copy of the interleaved primal fields (FieldPtrs::prim) in
-// shared memory, two float4 per cell, over nodes x0 .. x0 + w - 1 (and y, z)
+// A 3D tile's copy of the primal fields (FieldPtrs::prim) in shared memory
+// over nodes x0 .. x0 + w - 1 (and y, z): (pex, pey, pez, pbx) in a float4
+// array and (pby, pbz) in a float2 array, so that lanes at random cells
+// spread over every bank (a 32-byte cell stride would start every 16-byte
+// load on one of four bank groups)
 struct FieldWin3 {
-    const float4 *s;
+    const float4 *sa;
+    const float2 *sb;
     int x0, y0, z0, w, h, d;
 };
 
@@ -288,7 +293,8 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
 #pragma unroll
                 for (int r1 = 0; r1 < NS; r1++) {
                     const int l = row + r1;
-                    const float4 pa = win3->s[2 * l], pb = win3->s[2 * l + 1];
+                    const float4 pa = win3->sa[l];
+                    const float2 pb = win3->sb[l];
                     sx = sx + pa.x * axp[r1];
                     sy_ = sy_ + pa.y * axp[r1];
                     sz_ = sz_ + pa.z * axp[r1];

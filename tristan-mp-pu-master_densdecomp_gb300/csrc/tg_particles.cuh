@@ -712,7 +712,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     }
     // 3D: the interleaved primal copies over the gather's reach
     FieldWin3 fwin3;
-    fwin3.s = reinterpret_cast<const float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+    fwin3.sa = reinterpret_cast<const float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+    fwin3.sb = reinterpret_cast<const float2 *>(fwin3.sa + g.fwcells);
     fwin3.x0 = g.ox + tix * g.tx - g.fw_lo;
     fwin3.y0 = g.oy + tiy * g.ty - g.fw_lo;
     fwin3.z0 = g.oz + tiz * g.tz - g.fw_lo;
@@ -720,7 +721,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     fwin3.h = g.fwy;
     fwin3.d = g.fwz;
     if (DIM == 3 && PUSH && g.fwcells > 0) {
-        float4 *fs = reinterpret_cast<float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+        float4 *fa = reinterpret_cast<float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
+        float2 *fb = reinterpret_cast<float2 *>(fa + g.fwcells);
         for (int c = threadIdx.x; c < g.fwcells; c += blockDim.x) {
             const int i = fwin3.x0 + c % g.fwx, j = fwin3.y0 + (c / g.fwx) % g.fwy, k = fwin3.z0 + c / (g.fwx * g.fwy);
             float4 pa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), pb = pa;
@@ -729,8 +731,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                 pa = __ldg(a.f.prim + 2 * l);
                 pb = __ldg(a.f.prim + 2 * l + 1);
             }
-            fs[2 * c] = pa;
-            fs[2 * c + 1] = pb;
+            fa[c] = pa;
+            fb[c] = make_float2(pb.x, pb.y);
         }
     }
     if (DEPOSIT) {
