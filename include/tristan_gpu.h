@@ -87,7 +87,9 @@ typedef struct {
     int32_t fx_shift;    /* fixed-point scale 2^fx_shift */
     int64_t maxhlf;      /* particle capacity per species */
     int32_t sort_every;  /* re-sort particles into tiles every k laps (>= 1) */
-    int32_t tile[3];     /* tile edge in cells (0 = automatic) */
+    int32_t tile[3];     /* tile edge in cells (0 = automatic); a tile's shared
+                            memory (its deposit window and field copy) must fit
+                            in 227 KB, else tg_init fails with TG_ERR_ARG */
     int32_t device;      /* CUDA device ordinal */
     int32_t diag_every;  /* 1: FP64 diagnostics inside every tg_step lap */
 } tg_config;

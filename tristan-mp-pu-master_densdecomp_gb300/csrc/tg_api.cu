@@ -256,7 +256,7 @@ int tg::build_geom(const tg_config &c, Geom &g, char *err, size_t errlen) {
     }
     const size_t smem = tile_smem_bytes(c.dims, g.wcells, g.fwcells);  // window and field copy
     if (smem > 227 * 1024)
-        return geom_fail(err, errlen, "deposit window of %zu bytes exceeds shared memory; use smaller tiles", smem);
+        return geom_fail(err, errlen, "tile shared memory (deposit window and field copy) of %zu bytes exceeds 227 KB; use smaller tiles", smem);
     return TG_OK;
 }
 
