@@ -33,6 +33,7 @@ run N independent replicas and `value` sums them (weak scaling).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -256,12 +257,18 @@ def run_e2e(cfg, ions, lecs, e2e_steps, host_parts, device):
     # one tg_step_host call per lap: E, B and the records up, the lap,
     # everything back, as the reference's main loop would drive it
     laps = []
+    # the interpreter's cyclic garbage collector stays off while the laps
+    # are timed (a collection pass is the harness's pause, not the lap's)
+    gc_was = gc.isenabled()
+    gc.disable()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
         sim.step_host(1)
         laps.append((time.perf_counter() - t1) * 1e3)
     dt = time.perf_counter() - t0
+    if gc_was:
+        gc.enable()
     sim.close()
     return dt, h2d, d2h, huge, laps
 
