@@ -64,7 +64,7 @@ struct Geom {
     int wlo, whi;  // halo below / above the tile, same on every axis
     int wx, wy, wz;
     int wcells;
-    // 3D: the tile's copy of the interleaved primal fields over the gather's
+    // 3D: the tile's copy of the primal fields over the gather's
     // reach (fw_lo cells below the tile, fwx x fwy x fwz cells), when two
     // CTAs per SM still fit beside the deposit window (fwcells = 0: none)
     int fw_lo, fwx, fwy, fwz, fwcells;

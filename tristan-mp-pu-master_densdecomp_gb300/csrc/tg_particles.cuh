@@ -663,8 +663,9 @@ __device__ __forceinline__ void particle_step(const TileArgs &a, WindowSink<FIXE
 }
 
 // One tile: push, deposit into the shared window, wrap, flush. Every thread
-// of the CTA calls it with the same tile (it contains barriers); smem_raw is
-// the 6 * wcells words of the window.
+// of the CTA calls it with the same tile (it contains barriers); smem_raw
+// holds the window (6 * wcells words) and the tile's field copy
+// (tile_smem_bytes).
 template <int DIM, int ORDER, bool FIXED, bool PUSH, bool DEPOSIT>
 __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, unsigned char *smem_raw) {
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
@@ -710,7 +711,8 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
                     (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) ? __ldg(src[comp] + (i - 1) + g.sy * (j - 1)) : 0.0f;
             }
     }
-    // 3D: the interleaved primal copies over the gather's reach
+    // 3D: the primal copies over the gather's reach (a float4 and a float2
+    // array)
     FieldWin3 fwin3;
     fwin3.sa = reinterpret_cast<const float4 *>(smem_raw + tile_fieldwin_offset(g.wcells));
     fwin3.sb = reinterpret_cast<const float2 *>(fwin3.sa + g.fwcells);
