@@ -96,3 +96,12 @@ def test_struct_layouts_match_the_header(tmp_path):
         if "." in key:
             t, f = key.split(".")
             assert getattr(mirrors[t], f).offset == off, key
+
+
+def test_init_counts_the_2d_field_copy_in_shared_memory():
+    # 2D tiles carry the deposit window and a copy of the six field arrays
+    # over the same cells: a 72 x 72 order-3 tile (77 x 77 window cells,
+    # 142 KB each) fits one but not both in the 227 KB of a CTA
+    cfg = SimConfig(dims=2, order=3, nx=144, ny=144, maxhlf=1024, tile=(72, 72, 1), sort_every=1)
+    rc, msg = init_rc(cfg)
+    assert rc == gpu.TG_ERR_ARG and "shared memory" in msg and "field copy" in msg
