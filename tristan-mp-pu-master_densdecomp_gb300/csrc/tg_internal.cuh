@@ -206,10 +206,11 @@ struct FieldPtrs {
     const float4 *prim;
 };
 
-// A tile's copy of the six staggered 2D field arrays in shared memory
-// ([6][h][w]: ex, ey, ez, bx, by, bz) over nodes x0 .. x0 + w - 1,
-// y0 .. y0 + h - 1 (1-based), read by the gather of every particle whose
-// nodes lie inside it
+// A tile's copy of the six staggered 2D field arrays in shared memory over
+// nodes x0 .. x0 + w - 1, y0 .. y0 + h - 1 (1-based), read by the gather of
+// every particle whose nodes lie inside it. The components a gather node
+// reads at one cell are paired: (ex, by) and (ey, bx) as float2 arrays,
+// then ez and bz, w * h entries each.
 struct FieldWin {
     const float *s;
     int x0, y0, w, h;
@@ -343,8 +344,8 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
                jd - 3 + byd >= win->y0 && jp - 4 + byd + NS < win->y0 + win->h) {
         // every node in the tile's shared copy: the same loop on shared loads
         const int plane = win->w * win->h;
-        const float *sex = win->s, *sey = sex + plane, *sez = sey + plane;
-        const float *sbx = sez + plane, *sby = sbx + plane, *sbz = sby + plane;
+        const float2 *sxb = reinterpret_cast<const float2 *>(win->s), *syx = sxb + plane;
+        const float *sez = reinterpret_cast<const float *>(syx + plane), *sbz = sez + plane;
 #pragma unroll 1
         for (int r2 = 0; r2 < NS; r2++) {
             const int rowp = win->w * (jp - 3 + byd + r2 - win->y0);
@@ -355,11 +356,12 @@ __device__ __forceinline__ void push_particle(const Geom &g, const FieldPtrs &f,
                 const int colp = ip - 3 + bxd + r1 - win->x0;
                 const int cold = id - 3 + bxd + r1 - win->x0;
                 const int lpp = colp + rowp, lpd = colp + rowd, ldp = cold + rowp, ldd = cold + rowd;
-                ex0 = ex0 + sex[ldp] * wxd[r1] * ay;
-                ey0 = ey0 + sey[lpd] * axp[r1] * wy;
+                const float2 eb = sxb[ldp], yb = syx[lpd];
+                ex0 = ex0 + eb.x * wxd[r1] * ay;
+                ey0 = ey0 + yb.x * axp[r1] * wy;
                 ez0 = ez0 + sez[lpp] * axp[r1] * ay;
-                bx0 = bx0 + sbx[lpd] * axp[r1] * wy;
-                by0 = by0 + sby[ldp] * wxd[r1] * ay;
+                bx0 = bx0 + yb.y * axp[r1] * wy;
+                by0 = by0 + eb.y * wxd[r1] * ay;
                 bz0 = bz0 + sbz[ldd] * wxd[r1] * wy;
             }
         }

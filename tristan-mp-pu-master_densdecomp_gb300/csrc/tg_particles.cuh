@@ -701,15 +701,27 @@ __device__ __forceinline__ void tile_body(const TileArgs &a, const int tile, uns
     fwin.w = g.wx;
     fwin.h = g.wy;
     if (DIM == 2 && PUSH) {
-        float *fs = reinterpret_cast<float *>(smem_raw) + nwords;
-        const float *src[6] = {a.f.ex, a.f.ey, a.f.ez, a.f.bx, a.f.by, a.f.bz};
-#pragma unroll
-        for (int comp = 0; comp < 6; comp++)
-            for (int c = threadIdx.x; c < g.wcells; c += blockDim.x) {
-                const int i = fwin.x0 + c % g.wx, j = fwin.y0 + c / g.wx;
-                fs[comp * g.wcells + c] =
-                    (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) ? __ldg(src[comp] + (i - 1) + g.sy * (j - 1)) : 0.0f;
+        // (ex, by) and (ey, bx) pairs, then ez and bz (FieldWin)
+        float2 *fxb = reinterpret_cast<float2 *>(reinterpret_cast<float *>(smem_raw) + nwords);
+        float2 *fyx = fxb + g.wcells;
+        float *fez = reinterpret_cast<float *>(fyx + g.wcells), *fbz = fez + g.wcells;
+        for (int c = threadIdx.x; c < g.wcells; c += blockDim.x) {
+            const int i = fwin.x0 + c % g.wx, j = fwin.y0 + c / g.wx;
+            float v[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (i >= 1 && i <= g.mx && j >= 1 && j <= g.my) {
+                const long long l = (i - 1) + g.sy * (j - 1);
+                v[0] = __ldg(a.f.ex + l);
+                v[1] = __ldg(a.f.ey + l);
+                v[2] = __ldg(a.f.ez + l);
+                v[3] = __ldg(a.f.bx + l);
+                v[4] = __ldg(a.f.by + l);
+                v[5] = __ldg(a.f.bz + l);
             }
+            fxb[c] = make_float2(v[0], v[4]);
+            fyx[c] = make_float2(v[1], v[3]);
+            fez[c] = v[2];
+            fbz[c] = v[5];
+        }
     }
     // 3D: the primal copies over the gather's reach (a float4 and a float2
     // array)
