@@ -41,11 +41,16 @@ struct DiagArgs {
     int only;                   // 0 both species, 1 ions only, 2 electrons only
 };
 
-#ifndef TG_DIAG_MINB
-#define TG_DIAG_MINB 4
+// resident CTAs per SM the particle pass's registers are sized for, per
+// dimension
+#ifndef TG_DIAG_MINB_2D
+#define TG_DIAG_MINB_2D 4
+#endif
+#ifndef TG_DIAG_MINB_3D
+#define TG_DIAG_MINB_3D 4
 #endif
 template <int DIM, int ORDER>
-__global__ void __launch_bounds__(256, TG_DIAG_MINB) k_diag_particles(DiagArgs a) {
+__global__ void __launch_bounds__(256, DIM == 3 ? TG_DIAG_MINB_3D : TG_DIAG_MINB_2D) k_diag_particles(DiagArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned *winlo = reinterpret_cast<unsigned *>(smem_raw);
     int *winhi = reinterpret_cast<int *>(smem_raw) + a.g.wcells;
