@@ -105,3 +105,14 @@ def test_init_counts_the_2d_field_copy_in_shared_memory():
     cfg = SimConfig(dims=2, order=3, nx=144, ny=144, maxhlf=1024, tile=(72, 72, 1), sort_every=1)
     rc, msg = init_rc(cfg)
     assert rc == gpu.TG_ERR_ARG and "shared memory" in msg and "field copy" in msg
+
+
+def test_init_drops_the_3d_field_copy_rather_than_refusing():
+    # a 3D tile keeps its shared field copy only while two CTAs per SM fit
+    # beside the deposit window; when they would not (here the drift of a
+    # sort every second lap widens both), the copy is left out and the
+    # geometry stands (on a host without a GPU tg_init then stops at the
+    # device, past every argument check)
+    cfg = SimConfig(dims=3, order=2, nx=64, ny=64, nz=64, maxhlf=1024, tile=(16, 8, 4), sort_every=2)
+    rc, msg = init_rc(cfg)
+    assert rc != gpu.TG_ERR_ARG, msg
